@@ -1,0 +1,460 @@
+#!/usr/bin/env python
+"""SpMV benchmark: every format on the four seeded synthetic families, FP64
+and FP32, one GB300.
+
+A step is one SpMV (y = A*x, alpha=1, beta=0) of every feasible
+(family, format, precision) matrix of the workload:
+    families  banded_2M, powerlaw_4M, block4_2M, uniform_4M
+    formats   the library's formats (infeasible pairs are skipped and listed:
+              DIA over 10240 diagonals, ELL/BSR whose padded size exceeds 4x
+              the CSR size)
+    precision f64, f32
+value = sum of algorithmic bytes / sum of kernel time (GB/s), device-resident
+inputs, L2 flushed (256 MiB write) before every SpMV and excluded from the
+timing.  e2e = the same through the C ABI with pinned host x copied in and y
+copied out inside the timed region of every SpMV.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl sspmv|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+FAMILIES = ["banded_2M", "powerlaw_4M", "block4_2M", "uniform_4M"]
+DTYPES = ["f64", "f32"]
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="sspmv", choices=["sspmv", "reference"])
+    ap.add_argument("--families", default=",".join(FAMILIES))
+    ap.add_argument("--formats", default="all")
+    ap.add_argument("--dtypes", default=",".join(DTYPES))
+    ap.add_argument("--scale", type=float, default=1.0, help="row-count scale (testing only)")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def np_dtype(tag):
+    return np.float64 if tag == "f64" else np.float32
+
+
+def scaled_params(name, scale):
+    from sspmv_gb300 import synth
+    p = synth.WORKLOADS[name]()
+    if scale != 1.0:
+        if p.family == synth.LAPLACIAN2D:
+            p.grid = max(8, int(p.grid * scale ** 0.5))
+        else:
+            p.num_rows = max(4096, int(p.num_rows * scale))
+            if p.family == synth.BLOCK:
+                p.num_blocks = max(16, int(p.num_blocks * scale))
+    return p
+
+
+def host_matrices(families, scale):
+    from sspmv_gb300 import synth
+    mats = {}
+    for fam in families:
+        A = synth.generate(scaled_params(fam, scale), seed=1, dtype=np.float64)
+        mats[(fam, "f64")] = A
+        mats[(fam, "f32")] = A.astype(np.float32)
+    return mats
+
+
+# ------------------------------------------------------------------ clocks --
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        rows = [ln.split(",") for ln in Path(self.file.name).read_text().splitlines() if ln.count(",") >= 8]
+        os.unlink(self.file.name)
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_table():
+    """Per-launch DRAM bytes of the kernels measured with ncu (profiles/traffic.json)."""
+    p = ROOT / "profiles" / "traffic.json"
+    return json.loads(p.read_text()) if p.exists() else {}
+
+
+# ---------------------------------------------------------------- GPU arm --
+def run_gpu(args, rank, world):
+    import torch
+    from sspmv_gb300 import _lib
+    from sspmv_gb300 import lespmv as L
+
+    dev = torch.device("cuda", rank % max(1, torch.cuda.device_count()))
+    torch.cuda.set_device(dev)
+    families = [f for f in args.families.split(",") if f]
+    dtypes = [d for d in args.dtypes.split(",") if d]
+    fmts = L.FORMATS if args.formats == "all" else args.formats.split(",")
+    hosts = host_matrices(families, args.scale)
+
+    cases, skipped = [], []
+    for fam in families:
+        for dt in dtypes:
+            A = hosts[(fam, dt)]
+            csr = L.csr_from_host(A)
+            for fmt in fmts:
+                M, why = L.build_format(csr, fmt, A)
+                if M is None:
+                    skipped.append(f"{fam}/{fmt}/{dt}: {why}")
+                    continue
+                x = torch.from_numpy(_x_host(A.num_cols, dt)).to(dev)
+                y = torch.zeros(A.num_rows, dtype=x.dtype, device=dev)
+                cases.append({"fam": fam, "fmt": fmt, "dt": dt, "M": M, "x": x, "y": y,
+                              "bytes": M.algorithmic_bytes(1, False), "csr": csr, "nnz": A.nnz,
+                              "rows": A.num_rows, "cols": A.num_cols})
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def one_step(record):
+        for c in cases:
+            flush.zero_()
+            e0, e1 = record(c)
+            e0.record(stream)
+            L.LeSpMV(1.0, c["M"], c["x"], 0.0, c["y"], stream)
+            e1.record(stream)
+
+    for _ in range(args.warmup):
+        one_step(lambda c: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)))
+    torch.cuda.synchronize()
+
+    events = {id(c): [] for c in cases}
+
+    def rec(c):
+        pair = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        events[id(c)].append(pair)
+        return pair
+
+    sampler = ClockSampler(dev.index)
+    _barrier(world)
+    torch.cuda.synchronize()
+    sampler.start()
+    launches0 = _lib.lib.sspmv_launch_count()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        one_step(rec)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    launches = _lib.lib.sspmv_launch_count() - launches0
+    clocks = sampler.stop()
+    _barrier(world)
+
+    per_case = []
+    total_ms = 0.0
+    total_bytes = 0.0
+    for c in cases:
+        ms = [a.elapsed_time(b) for a, b in events[id(c)]]
+        avg = sum(ms) / len(ms)
+        total_ms += sum(ms)
+        total_bytes += c["bytes"] * len(ms)
+        per_case.append({"family": c["fam"], "format": c["fmt"], "dtype": c["dt"], "ms": round(avg, 5),
+                         "GBps": round(c["bytes"] / avg / 1e6, 1),
+                         "GFLOPs": round(2.0 * c["nnz"] / avg / 1e6, 1)})
+    step_ms = total_ms / args.steps
+    step_ms = _max_over_ranks(step_ms, world)
+    value = total_bytes / args.steps * world / (step_ms * 1e6)
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, cases, flush, stream, world)
+
+    dom = max(range(len(cases)), key=lambda i: per_case[i]["ms"])
+    dc = cases[dom]
+    peak, peak_kind = measured_peak()
+    ach = dc["bytes"] / per_case[dom]["ms"] / 1e6
+    tt = traffic_table().get(f"{dc['fam']}/{dc['fmt']}/{dc['dt']}")
+    roofline = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(ach / peak, 4), "peak_kind": peak_kind,
+                "traffic": tt["bytes_per_launch"] if tt else None,
+                "kernel": f"{dc['fam']}/{dc['fmt']}/{dc['dt']}",
+                "algorithmic_bytes": dc["bytes"]}
+    cpu = None
+    if rank == 0 and world == 1:
+        cpu = cpu_baseline(hosts, families, dtypes, fmts, budget_s=15.0)
+    return {
+        "metric": "SpMV GB/s (algorithmic bytes / kernel time), all formats x 4 families x {f64,f32}",
+        "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64+f32", "data": "synthetic (seeded generator, families of the SpMV suite)",
+        "config": {"workload": "spmv-suite: " + "+".join(families) + " x " + "+".join(fmts) + " x " + "+".join(dtypes),
+                   "l2": "flushed before every SpMV (256 MiB write), flush not timed",
+                   "alpha": 1.0, "beta": 0.0, "k_rhs": 1, "index": "int32", "parallelism": f"replicas{world}",
+                   "skipped": skipped, "scale": args.scale},
+        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches),
+        "wall_s": round(wall, 3), "per_format": per_case,
+    }
+
+
+def _x_host(n, dt):
+    from sspmv_gb300 import synth
+    return synth.vector(n, 0, np_dtype(dt))
+
+
+def run_e2e(args, cases, flush, stream, world):
+    """Same sweep through the public call with host buffers: pinned x copied
+    in, SpMV, y copied out, all inside the CUDA-event bracket of each SpMV."""
+    import torch
+    from sspmv_gb300 import lespmv as L
+    hx = [c["x"].cpu().pin_memory() for c in cases]
+    hy = [torch.empty(c["rows"], dtype=c["y"].dtype).pin_memory() for c in cases]
+    h2d = sum(t.numel() * t.element_size() for t in hx)
+    d2h = sum(t.numel() * t.element_size() for t in hy)
+    total_ms, total_bytes = 0.0, 0.0
+    for step in range(args.warmup + args.steps):
+        pairs = []
+        for i, c in enumerate(cases):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            c["x"].copy_(hx[i], non_blocking=True)
+            L.LeSpMV(1.0, c["M"], c["x"], 0.0, c["y"], stream)
+            hy[i].copy_(c["y"], non_blocking=True)
+            e1.record(stream)
+            pairs.append((e0, e1, c["bytes"]))
+        torch.cuda.synchronize()
+        if step >= args.warmup:
+            for e0, e1, b in pairs:
+                total_ms += e0.elapsed_time(e1)
+                total_bytes += b
+    step_ms = _max_over_ranks(total_ms / args.steps, world)
+    return {"value": round(total_bytes / args.steps * world / (step_ms * 1e6), 1), "unit": "GB/s",
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": round(step_ms, 4)}
+
+
+# ------------------------------------------------------------- CPU legs ----
+def cpu_sample(A, frac=0.125):
+    """First `frac` of the rows of A (all columns kept)."""
+    from sspmv_gb300.synth import HostCSR
+    r = max(1, int(A.num_rows * frac))
+    nnz = int(A.row_offset[r])
+    return HostCSR(r, A.num_cols, A.row_offset[:r + 1].copy(), A.col_index[:nnz], A.values[:nnz])
+
+
+def _cpu_convert(O, fmt, A):
+    """Oracle (CPU restatement) conversion of a sample for the CPU timing; None if infeasible."""
+    from sspmv_gb300.lespmv import feasible_host
+    ok, _ = feasible_host(fmt, A)
+    if not ok:
+        return None
+    if fmt == "csr" or fmt == "csr5":
+        return {}
+    if fmt == "coo":
+        return O.csr_to_coo(A)
+    if fmt == "ell":
+        d = O.csr_to_ell(A, 1)
+        d["ld"] = 1
+        return d
+    if fmt == "sell":
+        d = O.csr_to_sell(A, 4)
+        d["C"] = 4
+        return d
+    if fmt == "sell_c_sigma":
+        d = O.csr_to_sell_c_sigma(A, 16384, 4)
+        d["C"] = 4
+        return d
+    if fmt == "sell_c_R":
+        d = O.csr_to_sell_c_R(A, 4)
+        d["C"] = 4
+        return d
+    if fmt == "dia":
+        return O.csr_to_dia(A)
+    if fmt == "bsr":
+        from sspmv_gb300.lespmv import bsr_block_for
+        r, c = bsr_block_for(A)
+        return O.csr_to_bsr(A, r, c)
+    return None
+
+
+def _cpu_bytes(fmt, A, d, sv):
+    m, n, nnz = A.num_rows, A.num_cols, A.nnz
+    xb, yb = n * sv, m * sv
+    if fmt in ("csr", "csr5"):
+        return nnz * (sv + 4) + (m + 1) * 4 + xb + yb
+    if fmt == "coo":
+        return nnz * (sv + 8) + xb + yb
+    if fmt in ("ell", "sell"):
+        return nnz * (sv + 4) + xb + yb
+    if fmt in ("sell_c_sigma", "sell_c_R"):
+        return nnz * (sv + 4) + m * 4 + xb + yb
+    if fmt == "dia":
+        return nnz * sv + d["complete_ndiags"] * 8 + xb + yb
+    if fmt == "bsr":
+        return nnz * sv + d["nnzb"] * 4 + (d["mb"] + 1) * 4 + xb + yb
+    return nnz * (sv + 4) + xb + yb
+
+
+def cpu_sweep(hosts, families, dtypes, fmts, budget_s, frac=0.125):
+    """Times the oracle port's OpenMP SpMV kernels (all host threads) on the
+    first `frac` of the rows of every matrix.  Returns (GB/s, seconds, threads)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    from oracle import Oracle
+    O = Oracle()
+    threads = O.lib.oracle_max_threads()
+    prepared = []
+    for fam in families:
+        for dt in dtypes:
+            A = cpu_sample(hosts[(fam, dt)], frac)
+            for fmt in fmts:
+                d = _cpu_convert(O, fmt, A)
+                if d is None:
+                    continue
+                x = _x_host(A.num_cols, dt)
+                y = np.zeros(A.num_rows, np_dtype(dt))
+                prepared.append((fmt, A, d, x, y, _cpu_bytes(fmt, A, d, np.dtype(np_dtype(dt)).itemsize)))
+    tot_b, tot_t = 0.0, 0.0
+    t_start = time.perf_counter()
+    reps = 0
+    while True:
+        for fmt, A, d, x, y, b in prepared:
+            fmt_o = "csr" if fmt == "csr5" else fmt
+            t0 = time.perf_counter()
+            O.spmv(fmt_o, d, A, 1.0, x, 0.0, y)
+            tot_t += time.perf_counter() - t0
+            tot_b += b
+        reps += 1
+        if time.perf_counter() - t_start > budget_s or reps >= 50:
+            break
+    return tot_b / tot_t / 1e9, tot_t, threads, reps
+
+
+def cpu_baseline(hosts, families, dtypes, fmts, budget_s):
+    gbs, secs, threads, reps = cpu_sweep(hosts, families, dtypes, fmts, budget_s)
+    return {"value": round(gbs, 2), "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": f"first 1/8 of the rows of every matrix, {reps} sweep(s), {secs:.1f} s of SpMV time; "
+                      "oracle restatement of the reference's OpenMP kernels (csr5 timed as csr)"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    families = [f for f in args.families.split(",") if f]
+    dtypes = [d for d in args.dtypes.split(",") if d]
+    from sspmv_gb300 import lespmv as L
+    fmts = L.FORMATS if args.formats == "all" else args.formats.split(",")
+    hosts = host_matrices(families, args.scale)
+    for _ in range(args.warmup):
+        cpu_sweep(hosts, families, dtypes, fmts, budget_s=0.0)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        gbs, secs, threads, _ = cpu_sweep(hosts, families, dtypes, fmts, budget_s=0.0)
+        vals.append((gbs, secs))
+    gbs = sum(v[0] * v[1] for v in vals) / sum(v[1] for v in vals)
+    ms = sum(v[1] for v in vals) / len(vals) * 1e3
+    return {"impl": "reference",
+            "metric": "SpMV GB/s (algorithmic bytes / kernel time), all formats x 4 families x {f64,f32}",
+            "value": round(gbs, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64+f32", "data": "synthetic (seeded generator, families of the SpMV suite)",
+            "config": {"workload": "spmv-suite: " + "+".join(families) + " x " + "+".join(fmts) + " x " + "+".join(dtypes),
+                       "sample": "first 1/8 of the rows of every matrix", "wall_s": round(time.perf_counter() - t0, 2)},
+            "cpu_baseline": {"value": round(gbs, 2), "unit": "GB/s", "cores": threads, "kind": "port",
+                             "sample": "first 1/8 of the rows of every matrix, one sweep per step"},
+            "e2e": {"value": round(gbs, 2), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# ------------------------------------------------------------ distributed --
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return rank, world
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    args = parse_args()
+    rank, world = _dist()
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+        if out is not None:
+            print(json.dumps(out))
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    out = run_gpu(args, rank, world)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,181 @@
+/*
+ * sspmv.h -- C ABI of the GB300-native sparse SpMV library (libsspmv.so).
+ *
+ * Drop-in boundary for LeSpMV's per-format SpMV path.  The reference exposes
+ * C++ templates over <IndexType, ValueType>; this ABI exposes one plain-C
+ * entry point per reference routine with the value type carried at run time
+ * in the matrix struct (SSPMV_F32 / SSPMV_F64, int32 indices).
+ *
+ *   reference (LeSpMV project paths)                  this ABI
+ *   ------------------------------------------------  ---------------------------
+ *   struct <Fmt>_Matrix (include/sparse_format.h)     sspmv_<fmt> (device arrays)
+ *   coo_to_csr / csr_to_<fmt>                         sspmv_coo_to_csr /
+ *     (include/sparse_conversion.h)                     sspmv_csr_to_<fmt>
+ *   LeSpMV_<fmt>(alpha, A, x, beta, y)                sspmv_LeSpMV_<fmt>
+ *     (src/spmv_<fmt>.cpp)                            (+ sspmv_spmm_<fmt>, k RHS)
+ *   delete_host_matrix (include/sparse_format.h)      sspmv_delete_<fmt>
+ *   read_csr_matrix (utils/sparse_io.cpp)             sspmv_read_mtx
+ *
+ * Conventions
+ *  - All matrix arrays and x / y live in device memory (HBM).  Matrices made
+ *    by this library own their arrays; free them with sspmv_delete_<fmt>.
+ *  - Every call is ordered on the given CUDA stream.  SpMV / SpMM calls do not
+ *    synchronize; converters synchronize their stream (they size outputs).
+ *  - Errors are returned as sspmv_status; nothing exits or throws.  The text
+ *    of the last error of the calling thread is sspmv_last_error().
+ *  - Parameters passed as 0 take the reference's shipped defaults:
+ *    chunk width C = 4, sigma = 16384, alignment = 64 / sizeof(value),
+ *    BSR block = 16 x (64 / sizeof(value)), max_diags = 10240,
+ *    CSR5 sigma = 16, omega = 64 / sizeof(value)
+ *    (include/general_config.h:17-26, include/plat_config.h:20-25).
+ *  - y = alpha*A*x + beta*y for every row, including rows without nonzeros.
+ *    beta == 0 never reads y.
+ *  - SpMM: k right-hand sides, X is row-major num_cols x k with leading
+ *    dimension ldx >= k (X[col*ldx + r]); Y likewise with ldy.
+ */
+#ifndef SSPMV_H
+#define SSPMV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *sspmv_stream_t; /* == cudaStream_t */
+
+typedef enum {
+    SSPMV_OK = 0,
+    SSPMV_INVALID_ARG = 1,
+    SSPMV_INFEASIBLE = 2,       /* e.g. DIA over max_diags (reference exits) */
+    SSPMV_OUT_OF_MEMORY = 3,
+    SSPMV_BUDGET_EXCEEDED = 4,
+    SSPMV_DEVICE_TIMEOUT = 5,
+    SSPMV_CUDA_ERROR = 6,
+    SSPMV_NOT_SUPPORTED = 7
+} sspmv_status;
+
+typedef enum { SSPMV_F32 = 0, SSPMV_F64 = 1 } sspmv_value_type;
+typedef enum { SSPMV_ROW_MAJOR = 0, SSPMV_COL_MAJOR = 1 } sspmv_leading_dimension;
+
+/* Matrix_Features (include/sparse_format.h:50-68).  `partition` of the
+ * reference (CPU thread split) is replaced by `priv`: library-private device
+ * state (cached schedules, carry buffers), created on first use. */
+typedef struct {
+    int64_t num_rows;
+    int64_t num_cols;
+    int64_t num_nnzs;
+    double sparsity;
+    double time, gflops, gbytes;
+    int32_t tag;
+    int32_t kernel_flag; /* 0 = library default kernel; see each format */
+    int32_t value_type;  /* sspmv_value_type */
+    int32_t owns;        /* 1: arrays allocated by the library */
+    void *priv;
+} sspmv_features;
+
+/* COO_Matrix (include/sparse_format.h:77-86) */
+typedef struct {
+    sspmv_features f;
+    int32_t *row_index;
+    int32_t *col_index;
+    void *values;
+    int32_t row_sorted; /* 1 when row_index is non-decreasing */
+} sspmv_coo;
+
+/* CSR_Matrix (include/sparse_format.h:96-104) */
+typedef struct {
+    sspmv_features f;
+    int32_t *row_offset;
+    int32_t *col_index;
+    void *values;
+} sspmv_csr;
+
+/* ---------------- status / memory ---------------- */
+const char *sspmv_status_string(sspmv_status s);
+const char *sspmv_last_error(void);
+const char *sspmv_version(void);
+/* Number of kernels this library has launched in the process so far. */
+int64_t sspmv_launch_count(void);
+
+/* ---------------- CSR creation ---------------- */
+/* Device CSR from arrays.  from_host != 0: copies host arrays to library-
+ * owned device memory.  from_host == 0: copies device arrays. */
+sspmv_status sspmv_csr_create(sspmv_csr *out, int32_t value_type, int64_t num_rows, int64_t num_cols,
+                              int64_t num_nnzs, const int32_t *row_offset, const int32_t *col_index,
+                              const void *values, int32_t from_host, sspmv_stream_t stream);
+/* Wrap caller-owned device arrays (nothing copied, nothing freed). */
+sspmv_status sspmv_csr_wrap(sspmv_csr *out, int32_t value_type, int64_t num_rows, int64_t num_cols,
+                            int64_t num_nnzs, int32_t *row_offset, int32_t *col_index, void *values);
+/* Copy the CSR arrays to host buffers (row_offset: num_rows+1, col_index and
+ * values: num_nnzs). */
+sspmv_status sspmv_csr_export(const sspmv_csr *A, int32_t *row_offset, int32_t *col_index, void *values,
+                              sspmv_stream_t stream);
+sspmv_status sspmv_delete_csr(sspmv_csr *A);
+
+/* ---------------- SpMV / SpMM ---------------- */
+/* LeSpMV_csr (src/spmv_csr.cpp:165-185).  kernel_flag 0/2: nnz-balanced
+ * merge-path kernel; 1: vector-per-row kernel. */
+sspmv_status sspmv_LeSpMV_csr(double alpha, const sspmv_csr *A, const void *x, double beta, void *y,
+                              sspmv_stream_t stream);
+sspmv_status sspmv_spmm_csr(double alpha, const sspmv_csr *A, int32_t k, const void *X, int64_t ldx,
+                            double beta, void *Y, int64_t ldy, sspmv_stream_t stream);
+
+/* Algorithmic bytes of one SpMV with k right-hand sides: structural bytes of
+ * the format (padding excluded) + x once + y once (twice when beta != 0). */
+double sspmv_algorithmic_bytes_csr(const sspmv_csr *A, int32_t k, int32_t beta_nonzero);
+
+/* ---------------- host utilities ---------------- */
+/* Matrix Market reader (utils/sparse_io.cpp:27-204: coordinate format,
+ * general/symmetric, real/integer/pattern; symmetric entries mirrored,
+ * duplicates kept, CSR built by a stable counting sort).  Two calls: first
+ * with NULL arrays to get sizes, then with buffers of those sizes. */
+sspmv_status sspmv_read_mtx(const char *path, int32_t value_type, int64_t *num_rows, int64_t *num_cols,
+                            int64_t *num_nnzs, int32_t *row_offset, int32_t *col_index, void *values);
+
+/* Writes a CSR matrix as "matrix coordinate real general" (1-based, %.17g),
+ * a file the reference's read_csr_matrix reads back bit-exactly. */
+sspmv_status sspmv_write_mtx(const char *path, int64_t num_rows, int64_t num_cols, const int32_t *row_offset,
+                             const int32_t *col_index, const double *values);
+
+typedef enum {
+    SSPMV_SYNTH_LAPLACIAN2D = 0,
+    SSPMV_SYNTH_BANDED = 1,
+    SSPMV_SYNTH_POWERLAW = 2,
+    SSPMV_SYNTH_BLOCK = 3,
+    SSPMV_SYNTH_UNIFORM = 4
+} sspmv_synth_family;
+
+typedef struct {
+    int32_t family;        /* sspmv_synth_family */
+    int32_t num_offsets;   /* BANDED */
+    int64_t num_rows;      /* all but LAPLACIAN2D */
+    int64_t num_cols;      /* 0: square */
+    int64_t grid;          /* LAPLACIAN2D: g (num_rows = g*g) */
+    int64_t offsets[32];   /* BANDED */
+    double alpha;          /* POWERLAW Zipf exponent */
+    double mean;           /* POWERLAW target mean row length (<=0: unscaled) */
+    int64_t cap;           /* POWERLAW maximum row length */
+    int64_t block_dim;     /* BLOCK: b */
+    int64_t num_blocks;    /* BLOCK: distinct dense blocks */
+    int64_t per_row;       /* UNIFORM */
+    double empty_row_frac; /* POWERLAW / UNIFORM: fraction of empty rows */
+} sspmv_synth_params;
+
+/* Seeded synthetic CSR: row offsets first (returns nnz, or -1 if it does not
+ * fit int32), then columns and values (FP32 values are the FP64 draws
+ * rounded). */
+int64_t sspmv_synth_row_offsets(const sspmv_synth_params *p, uint64_t seed, int32_t *row_offset);
+int sspmv_synth_fill_f64(const sspmv_synth_params *p, uint64_t seed, const int32_t *row_offset,
+                         int32_t *col_index, double *values);
+int sspmv_synth_fill_f32(const sspmv_synth_params *p, uint64_t seed, const int32_t *row_offset,
+                         int32_t *col_index, float *values);
+/* x_i ~ U[-1,1) from (seed, i). */
+void sspmv_synth_vector_f64(int64_t n, uint64_t seed, double *out);
+void sspmv_synth_vector_f32(int64_t n, uint64_t seed, float *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SSPMV_H */

@@ -1,0 +1,108 @@
+"""ctypes binding of libsspmv.so (include/sspmv.h).
+
+The library is built in-tree (sspmv_gb300/lib/libsspmv.so).  Importing this
+module fails loudly when the library is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+_LIB_PATH = Path(__file__).resolve().parent / "lib" / "libsspmv.so"
+
+F32, F64 = 0, 1
+ROW_MAJOR, COL_MAJOR = 0, 1
+
+STATUS = {0: "SSPMV_OK", 1: "SSPMV_INVALID_ARG", 2: "SSPMV_INFEASIBLE", 3: "SSPMV_OUT_OF_MEMORY",
+          4: "SSPMV_BUDGET_EXCEEDED", 5: "SSPMV_DEVICE_TIMEOUT", 6: "SSPMV_CUDA_ERROR",
+          7: "SSPMV_NOT_SUPPORTED"}
+
+
+class SSPMVError(RuntimeError):
+    def __init__(self, status: int, where: str, detail: str):
+        super().__init__(f"{where}: {STATUS.get(status, status)}: {detail}")
+        self.status = status
+
+
+class Features(C.Structure):
+    _fields_ = [("num_rows", C.c_int64), ("num_cols", C.c_int64), ("num_nnzs", C.c_int64),
+                ("sparsity", C.c_double), ("time", C.c_double), ("gflops", C.c_double),
+                ("gbytes", C.c_double), ("tag", C.c_int32), ("kernel_flag", C.c_int32),
+                ("value_type", C.c_int32), ("owns", C.c_int32), ("priv", C.c_void_p)]
+
+
+P32 = C.POINTER(C.c_int32)
+
+
+class Coo(C.Structure):
+    _fields_ = [("f", Features), ("row_index", P32), ("col_index", P32), ("values", C.c_void_p),
+                ("row_sorted", C.c_int32)]
+
+
+class Csr(C.Structure):
+    _fields_ = [("f", Features), ("row_offset", P32), ("col_index", P32), ("values", C.c_void_p)]
+
+
+class SynthParams(C.Structure):
+    _fields_ = [("family", C.c_int32), ("num_offsets", C.c_int32), ("num_rows", C.c_int64),
+                ("num_cols", C.c_int64), ("grid", C.c_int64), ("offsets", C.c_int64 * 32),
+                ("alpha", C.c_double), ("mean", C.c_double), ("cap", C.c_int64),
+                ("block_dim", C.c_int64), ("num_blocks", C.c_int64), ("per_row", C.c_int64),
+                ("empty_row_frac", C.c_double)]
+
+
+def _load():
+    if not _LIB_PATH.exists():
+        raise ImportError(f"libsspmv.so is not built ({_LIB_PATH}); run __graft_entry__.build() "
+                          "or python -m sspmv_gb300.build")
+    return C.CDLL(str(_LIB_PATH))
+
+
+lib = _load()
+
+_st = C.c_int
+_vp = C.c_void_p
+_i64 = C.c_int64
+_i32 = C.c_int32
+_d = C.c_double
+
+_SIGS = {
+    "sspmv_status_string": (C.c_char_p, [_st]),
+    "sspmv_last_error": (C.c_char_p, []),
+    "sspmv_version": (C.c_char_p, []),
+    "sspmv_launch_count": (_i64, []),
+    "sspmv_csr_create": (_st, [C.POINTER(Csr), _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp]),
+    "sspmv_csr_wrap": (_st, [C.POINTER(Csr), _i32, _i64, _i64, _i64, _vp, _vp, _vp]),
+    "sspmv_csr_export": (_st, [C.POINTER(Csr), _vp, _vp, _vp, _vp]),
+    "sspmv_delete_csr": (_st, [C.POINTER(Csr)]),
+    "sspmv_LeSpMV_csr": (_st, [_d, C.POINTER(Csr), _vp, _d, _vp, _vp]),
+    "sspmv_spmm_csr": (_st, [_d, C.POINTER(Csr), _i32, _vp, _i64, _d, _vp, _i64, _vp]),
+    "sspmv_algorithmic_bytes_csr": (_d, [C.POINTER(Csr), _i32, _i32]),
+    "sspmv_read_mtx": (_st, [C.c_char_p, _i32, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64), _vp, _vp, _vp]),
+    "sspmv_write_mtx": (_st, [C.c_char_p, _i64, _i64, _vp, _vp, _vp]),
+    "sspmv_synth_row_offsets": (_i64, [C.POINTER(SynthParams), C.c_uint64, _vp]),
+    "sspmv_synth_fill_f64": (C.c_int, [C.POINTER(SynthParams), C.c_uint64, _vp, _vp, _vp]),
+    "sspmv_synth_fill_f32": (C.c_int, [C.POINTER(SynthParams), C.c_uint64, _vp, _vp, _vp]),
+    "sspmv_synth_vector_f64": (None, [_i64, C.c_uint64, _vp]),
+    "sspmv_synth_vector_f32": (None, [_i64, C.c_uint64, _vp]),
+}
+
+
+def register(name: str, restype, argtypes) -> None:
+    fn = getattr(lib, name)
+    fn.restype = restype
+    fn.argtypes = argtypes
+
+
+for _n, (_r, _a) in _SIGS.items():
+    register(_n, _r, _a)
+
+
+def check(status: int, where: str) -> None:
+    if status != 0:
+        detail = lib.sspmv_last_error().decode(errors="replace")
+        raise SSPMVError(status, where, detail)
+
+
+def call(name: str, *args) -> None:
+    check(getattr(lib, name)(*args), name)

@@ -1,0 +1,94 @@
+"""In-tree build of libsspmv.so (sm_103a) and of the CPU oracle.
+
+`build_library()` compiles every source under sspmv_gb300/csrc with nvcc for
+sm_103a only (one -gencode), in parallel, into sspmv_gb300/_build/, and links
+sspmv_gb300/lib/libsspmv.so.  Objects are rebuilt when a source or header is
+newer than the object.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIBDIR = PKG / "lib"
+LIB = LIBDIR / "libsspmv.so"
+NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-std=c++17", "-lineinfo", f"-I{ROOT / 'include'}", f"-I{CSRC}",
+          "-Xcompiler", "-fPIC,-fopenmp,-Wall,-Wno-unused-function"]
+
+
+def _sources():
+    return sorted([p for p in CSRC.iterdir() if p.suffix in (".cu", ".cpp")])
+
+
+def _headers():
+    hs = [p for p in CSRC.iterdir() if p.suffix in (".cuh", ".h", ".inc")]
+    hs += list((ROOT / "include").glob("*.h"))
+    return hs
+
+
+def _stale(obj: Path, src: Path, newest_header: float) -> bool:
+    if not obj.exists():
+        return True
+    t = obj.stat().st_mtime
+    return src.stat().st_mtime > t or newest_header > t
+
+
+def _compile(src: Path, extra: list[str]) -> tuple[Path, str]:
+    obj = BUILD / (src.name + ".o")
+    cmd = [NVCC, *ARCH, *COMMON, *extra, "-c", str(src), "-o", str(obj)]
+    if src.suffix == ".cpp":
+        cmd = [NVCC, *COMMON, *extra, "-x", "c++", "-c", str(src), "-o", str(obj)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return obj, r.stderr
+
+
+def build_library(verbose: bool = False, extra: list[str] | None = None, jobs: int | None = None) -> Path:
+    extra = list(extra or [])
+    BUILD.mkdir(exist_ok=True)
+    LIBDIR.mkdir(exist_ok=True)
+    srcs = _sources()
+    newest = max((h.stat().st_mtime for h in _headers()), default=0.0)
+    todo = [s for s in srcs if _stale(BUILD / (s.name + ".o"), s, newest)]
+    jobs = jobs or min(len(todo) or 1, os.cpu_count() or 4)
+    with ThreadPoolExecutor(max_workers=jobs) as ex:
+        for obj, err in ex.map(lambda s: _compile(s, extra), todo):
+            if verbose:
+                print(f"[sspmv] built {obj.name}", file=sys.stderr)
+                if err.strip():
+                    print(err, file=sys.stderr)
+    objs = [BUILD / (s.name + ".o") for s in srcs]
+    if todo or not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
+        cmd = [NVCC, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-Xcompiler", "-fopenmp", "-lgomp"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return LIB
+
+
+def build_oracle(with_reference: bool | None = None) -> None:
+    """CPU oracle (test infrastructure): oracle/liboracle.so, plus the
+    reference harness oracle/_ref/libref.so when the reference sources exist."""
+    od = ROOT / "oracle"
+    subprocess.run(["make", "-s", "-C", str(od)], check=True)
+    ref_root = os.environ.get("SSPMV_REF_ROOT", "/root/reference")
+    if with_reference is None:
+        with_reference = Path(ref_root, "LeSpMV", "include").is_dir()
+    if with_reference:
+        subprocess.run(["make", "-s", "-C", str(od), "ref", f"REF_ROOT={ref_root}"], check=True)
+
+
+if __name__ == "__main__":
+    print(build_library(verbose=True))
+    build_oracle()

@@ -1,0 +1,110 @@
+// common.cuh -- shared internals of libsspmv: status/error plumbing, value
+// type dispatch, device memory helpers and small device utilities.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "sspmv.h"
+
+namespace sspmv {
+
+// ---------------------------------------------------------------- errors --
+void set_error(const char *fmt, ...);
+sspmv_status fail(sspmv_status s, const char *fmt, ...);
+
+#define SSPMV_CUDA_TRY(expr)                                                            \
+    do {                                                                                \
+        cudaError_t e_ = (expr);                                                        \
+        if (e_ != cudaSuccess) {                                                        \
+            return ::sspmv::fail(e_ == cudaErrorMemoryAllocation ? SSPMV_OUT_OF_MEMORY \
+                                                                 : SSPMV_CUDA_ERROR,    \
+                                 "%s:%d %s: %s", __FILE__, __LINE__, #expr,             \
+                                 cudaGetErrorString(e_));                               \
+        }                                                                               \
+    } while (0)
+
+// Every kernel launch of the library is counted (sspmv_launch_count).
+void note_launch();
+
+#define SSPMV_LAUNCH_CHECK()                 \
+    do {                                     \
+        ::sspmv::note_launch();              \
+        SSPMV_CUDA_TRY(cudaGetLastError());  \
+    } while (0)
+
+#define SSPMV_TRY(expr)                         \
+    do {                                        \
+        sspmv_status s_ = (expr);               \
+        if (s_ != SSPMV_OK) return s_;          \
+    } while (0)
+
+inline cudaStream_t cu(sspmv_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// ---------------------------------------------------------------- memory --
+// Library-owned device allocations are stream ordered (cudaMallocAsync).
+template <typename T>
+sspmv_status dalloc(T **p, size_t count, sspmv_stream_t s) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    SSPMV_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(p), count * sizeof(T), cu(s)));
+    return SSPMV_OK;
+}
+inline void dfree(void *p, sspmv_stream_t s) {
+    if (p) cudaFreeAsync(p, cu(s));
+}
+
+inline size_t vsize(int32_t vt) { return vt == SSPMV_F64 ? 8 : 4; }
+inline int default_alignment(int32_t vt) { return 64 / (int)vsize(vt); }  // SIMD_WIDTH/8/sizeof(V)
+
+inline bool valid_vt(int32_t vt) { return vt == SSPMV_F32 || vt == SSPMV_F64; }
+
+// Calls f.template operator()<V>() with V = float or double.
+template <typename F>
+sspmv_status dispatch_value(int32_t vt, F &&f) {
+    if (vt == SSPMV_F64) return f((double)0);
+    if (vt == SSPMV_F32) return f((float)0);
+    return fail(SSPMV_INVALID_ARG, "unknown value_type %d", vt);
+}
+
+inline int num_sms() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 152;
+    }
+    return n;
+}
+
+inline unsigned grid_for(int64_t work, int block, int64_t cap = 0) {
+    int64_t g = (work + block - 1) / block;
+    if (g < 1) g = 1;
+    if (cap > 0 && g > cap) g = cap;
+    if (g > 0x7fffffff) g = 0x7fffffff;
+    return (unsigned)g;
+}
+
+// --------------------------------------------------------- device helpers --
+// Streaming (evict-first) loads for matrix arrays that are read once per SpMV.
+template <typename T>
+__device__ __forceinline__ T ld_stream(const T *p) { return __ldcs(p); }
+// Read-only cached loads for the gathered vector.
+template <typename T>
+__device__ __forceinline__ T ld_x(const T *p) { return __ldg(p); }
+
+template <typename V>
+__device__ __forceinline__ V axpby(V alpha, V sum, V beta, const V *y) {
+    return beta == V(0) ? alpha * sum : alpha * sum + beta * *y;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v, unsigned width = 32) {
+    for (unsigned o = width / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, width);
+    return v;
+}
+
+}  // namespace sspmv

@@ -1,0 +1,404 @@
+// spmv_csr.cu -- CSR SpMV / SpMM on sm_103a.
+//
+// Replaces LeSpMV_csr (src/spmv_csr.cpp:165-185) and its three CPU kernels
+// (serial, OpenMP per row, nnz-balanced row partition).
+//
+// Default kernel (kernel_flag 0 or 2): merge-path.  The (row end, nonzero)
+// merge sequence is cut into equal tiles of kTile items, so every CTA does the
+// same work whatever the row lengths (power-law rows up to 50k nonzeros and
+// empty rows alike).  A CTA stages its nonzeros' products a_ij * x_j into
+// shared memory with coalesced streaming loads, then each thread walks
+// kItems merge items and writes the rows it finishes.  Row pieces that cross
+// thread boundaries are joined by a block-wide segmented scan; rows that cross
+// tile boundaries leave (row, partial) carries in the plan and are finished by
+// a second kernel, in a fixed order, so results are deterministic.
+//
+// kernel_flag 1: vector-per-row kernel, `lanes` threads per row (2..32,
+// chosen from the mean row length, or set by the autotuner).
+#include "common.cuh"
+#include "plan.cuh"
+
+namespace sspmv {
+namespace {
+
+constexpr int kBlock = 256;
+
+template <int K>
+struct MergeShape {
+    static constexpr int items = K <= 4 ? 8 : 4;     // merge items per thread
+    static constexpr int tile = kBlock * items;       // 2048 or 1024
+    static constexpr int which = K <= 4 ? 0 : 1;
+};
+
+__global__ void merge_path_search(int64_t num_tiles, int tile_items, int m, int nnz,
+                                  const int32_t *__restrict__ row_offset, int2 *__restrict__ coords) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > num_tiles) return;
+    int64_t total = (int64_t)m + nnz;
+    int64_t d = t * tile_items;
+    if (d > total) d = total;
+    int64_t lo = d - nnz > 0 ? d - nnz : 0;
+    int64_t hi = d < m ? d : m;
+    while (lo < hi) {
+        int64_t p = (lo + hi) >> 1;
+        if ((int64_t)row_offset[p + 1] <= d - p - 1) lo = p + 1;
+        else hi = p;
+    }
+    coords[t] = make_int2((int)lo, (int)(d - lo));
+}
+
+template <typename V, int K>
+struct alignas(16) VecK {
+    V v[K];
+};
+
+template <typename V, int K>
+__global__ void __launch_bounds__(kBlock) csr_merge_kernel(
+    int m, const int32_t *__restrict__ row_offset, const int32_t *__restrict__ col_index,
+    const V *__restrict__ values, const V *__restrict__ x, int64_t ldx, V alpha, V beta,
+    V *__restrict__ y, int64_t ldy, const int2 *__restrict__ coords, int32_t *__restrict__ carry_row,
+    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val) {
+    constexpr int kItems = MergeShape<K>::items;
+    constexpr int kTile = MergeShape<K>::tile;
+    constexpr int kWarps = kBlock / 32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    V *s_prod = reinterpret_cast<V *>(smem_raw);                     // kTile * K
+    int *s_rowend = reinterpret_cast<int *>(s_prod + kTile * K);      // kTile + 1
+    __shared__ int s_wkey[kWarps];
+    __shared__ V s_wval[kWarps][K];
+    __shared__ V s_wpref[kWarps][K];
+    __shared__ V s_full[kBlock][K];
+    __shared__ int s_row0_start;
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t t = blockIdx.x;
+    const int2 c0 = coords[t], c1 = coords[t + 1];
+    const int i0 = c0.x, j0 = c0.y;
+    const int nrows = c1.x - i0, nnzs = c1.y - j0;
+
+    // ---- stage row ends and products (coalesced, streaming) ----
+    for (int k = tid; k < nrows; k += kBlock) s_rowend[k] = ld_stream(row_offset + i0 + 1 + k);
+    if (tid == 0) s_row0_start = i0 < m ? row_offset[i0] : 0;
+    for (int k = tid; k < nnzs; k += kBlock) {
+        const int c = ld_stream(col_index + j0 + k);
+        const V a = ld_stream(values + j0 + k);
+        const V *xp = x + (int64_t)c * ldx;
+#pragma unroll
+        for (int r = 0; r < K; r++) s_prod[k * K + r] = a * ld_x(xp + r);
+    }
+    __syncthreads();
+
+    // ---- per-thread merge over kItems items ----
+    const int total = nrows + nnzs;
+    const int d = min(tid * kItems, total);
+    int lo = max(d - nnzs, 0), hi = min(d, nrows);
+    while (lo < hi) {
+        int p = (lo + hi) >> 1;
+        if (s_rowend[p] <= j0 + d - p - 1) lo = p + 1;
+        else hi = p;
+    }
+    int ti = lo, tj = d - lo;
+    V sum[K];
+#pragma unroll
+    for (int r = 0; r < K; r++) sum[r] = V(0);
+    int first_row = -1;
+    V first_val[K];
+#pragma unroll
+    for (int r = 0; r < K; r++) first_val[r] = V(0);
+#pragma unroll
+    for (int s = 0; s < kItems; s++) {
+        if (ti < nrows && (tj >= nnzs || s_rowend[ti] <= j0 + tj)) {
+            if (first_row < 0) {
+                first_row = ti;
+#pragma unroll
+                for (int r = 0; r < K; r++) first_val[r] = sum[r];
+            } else {
+                V *yp = y + (int64_t)(i0 + ti) * ldy;
+#pragma unroll
+                for (int r = 0; r < K; r++) yp[r] = axpby(alpha, sum[r], beta, yp + r);
+            }
+#pragma unroll
+            for (int r = 0; r < K; r++) sum[r] = V(0);
+            ti++;
+        } else if (tj < nnzs) {
+#pragma unroll
+            for (int r = 0; r < K; r++) sum[r] += s_prod[tj * K + r];
+            tj++;
+        }
+    }
+
+    // ---- block-wide segmented inclusive scan of carry-outs keyed by row ----
+    int key = i0 + ti;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int k2 = __shfl_up_sync(0xffffffffu, key, o);
+        V v2[K];
+#pragma unroll
+        for (int r = 0; r < K; r++) v2[r] = __shfl_up_sync(0xffffffffu, sum[r], o);
+        if (lane >= o && k2 == key) {
+#pragma unroll
+            for (int r = 0; r < K; r++) sum[r] += v2[r];
+        }
+    }
+    if (lane == 31) {
+        s_wkey[warp] = key;
+#pragma unroll
+        for (int r = 0; r < K; r++) s_wval[warp][r] = sum[r];
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (int w = 0; w < kWarps; w++) {
+            bool join = w > 0 && s_wkey[w] == s_wkey[w - 1];
+#pragma unroll
+            for (int r = 0; r < K; r++) s_wpref[w][r] = s_wval[w][r] + (join ? s_wpref[w - 1][r] : V(0));
+        }
+    }
+    __syncthreads();
+    if (warp > 0 && key == s_wkey[warp - 1]) {
+#pragma unroll
+        for (int r = 0; r < K; r++) sum[r] += s_wpref[warp - 1][r];
+    }
+#pragma unroll
+    for (int r = 0; r < K; r++) s_full[tid][r] = sum[r];
+    __syncthreads();
+
+    if (first_row >= 0) {
+        V tot[K];
+#pragma unroll
+        for (int r = 0; r < K; r++) tot[r] = first_val[r] + (tid > 0 ? s_full[tid - 1][r] : V(0));
+        if (first_row == 0 && s_row0_start < j0) {
+            V *hp = head_val + t * kMaxK;
+#pragma unroll
+            for (int r = 0; r < K; r++) hp[r] = tot[r];
+        } else {
+            V *yp = y + (int64_t)(i0 + first_row) * ldy;
+#pragma unroll
+            for (int r = 0; r < K; r++) yp[r] = axpby(alpha, tot[r], beta, yp + r);
+        }
+    }
+    if (tid == kBlock - 1) {
+        carry_row[t] = key;
+        has_end[t] = nrows > 0;
+        V *cp = carry_val + t * kMaxK;
+#pragma unroll
+        for (int r = 0; r < K; r++) cp[r] = sum[r];
+    }
+}
+
+// Finishes rows that cross tile boundaries: the tile where such a row starts
+// owns it and adds the following tiles' pieces in order.
+template <typename V, int K>
+__global__ void csr_merge_fixup(int64_t num_tiles, int m, const int32_t *__restrict__ row_offset,
+                                const int2 *__restrict__ coords, const int32_t *__restrict__ carry_row,
+                                const int32_t *__restrict__ has_end, const V *__restrict__ carry_val,
+                                const V *__restrict__ head_val, V alpha, V beta, V *__restrict__ y,
+                                int64_t ldy) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= num_tiles) return;
+    const int r = carry_row[t];
+    if (r >= m) return;
+    const int rs = row_offset[r];
+    if (rs < coords[t].y || rs >= coords[t + 1].y) return;
+    V tot[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) tot[q] = carry_val[t * kMaxK + q];
+    for (int64_t u = t + 1; u < num_tiles; u++) {
+        if (has_end[u]) {
+#pragma unroll
+            for (int q = 0; q < K; q++) tot[q] += head_val[u * kMaxK + q];
+            break;
+        }
+#pragma unroll
+        for (int q = 0; q < K; q++) tot[q] += carry_val[u * kMaxK + q];
+    }
+    V *yp = y + (int64_t)r * ldy;
+#pragma unroll
+    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
+}
+
+template <typename V, int K, int VS>
+__global__ void __launch_bounds__(kBlock) csr_vector_kernel(
+    int m, const int32_t *__restrict__ row_offset, const int32_t *__restrict__ col_index,
+    const V *__restrict__ values, const V *__restrict__ x, int64_t ldx, V alpha, V beta,
+    V *__restrict__ y, int64_t ldy) {
+    constexpr int kRowsPerWarp = 32 / VS;
+    const int lane = threadIdx.x & 31;
+    const int sub = lane % VS;
+    const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp_id * kRowsPerWarp; base < m; base += nwarps * kRowsPerWarp) {
+        const int64_t row = base + lane / VS;
+        V s[K];
+#pragma unroll
+        for (int r = 0; r < K; r++) s[r] = V(0);
+        if (row < m) {
+            const int rs = ld_stream(row_offset + row), re = ld_stream(row_offset + row + 1);
+            for (int j = rs + sub; j < re; j += VS) {
+                const int c = ld_stream(col_index + j);
+                const V a = ld_stream(values + j);
+#pragma unroll
+                for (int r = 0; r < K; r++) s[r] += a * ld_x(x + (int64_t)c * ldx + r);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < K; r++) s[r] = warp_sum(s[r], VS);
+        if (row < m && sub == 0) {
+            V *yp = y + row * ldy;
+#pragma unroll
+            for (int r = 0; r < K; r++) yp[r] = axpby(alpha, s[r], beta, yp + r);
+        }
+    }
+}
+
+template <typename V, int K>
+sspmv_status launch_merge(const sspmv_csr *A, Plan *p, V alpha, const V *x, int64_t ldx, V beta, V *y,
+                          int64_t ldy, sspmv_stream_t s) {
+    constexpr int which = MergeShape<K>::which;
+    SSPMV_TRY(ensure_merge_plan(p, which, A->f.num_rows, A->f.num_nnzs, A->row_offset, A->f.value_type, s));
+    MergePlan &mp = p->merge[which];
+    const size_t smem = (size_t)MergeShape<K>::tile * K * sizeof(V) + ((size_t)MergeShape<K>::tile + 1) * 4;
+    static bool attr_set = false;
+    if (!attr_set) {
+        SSPMV_CUDA_TRY(cudaFuncSetAttribute(csr_merge_kernel<V, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem));
+        attr_set = true;
+    }
+    csr_merge_kernel<V, K><<<(unsigned)mp.num_tiles, kBlock, smem, cu(s)>>>(
+        (int)A->f.num_rows, A->row_offset, A->col_index, (const V *)A->values, x, ldx, alpha, beta, y, ldy,
+        mp.coords, mp.carry_row, mp.has_end, (V *)mp.carry_val, (V *)mp.head_val);
+    SSPMV_LAUNCH_CHECK();
+    if (mp.num_tiles > 1) {
+        csr_merge_fixup<V, K><<<grid_for(mp.num_tiles, 256), 256, 0, cu(s)>>>(
+            mp.num_tiles, (int)A->f.num_rows, A->row_offset, mp.coords, mp.carry_row, mp.has_end,
+            (const V *)mp.carry_val, (const V *)mp.head_val, alpha, beta, y, ldy);
+        SSPMV_LAUNCH_CHECK();
+    }
+    return SSPMV_OK;
+}
+
+template <typename V, int K, int VS>
+sspmv_status launch_vector_vs(const sspmv_csr *A, V alpha, const V *x, int64_t ldx, V beta, V *y, int64_t ldy,
+                              sspmv_stream_t s) {
+    const int64_t m = A->f.num_rows;
+    const int64_t warps = (m + (32 / VS) - 1) / (32 / VS);
+    const unsigned grid = grid_for(warps * 32, kBlock, (int64_t)num_sms() * 16);
+    csr_vector_kernel<V, K, VS><<<grid, kBlock, 0, cu(s)>>>((int)m, A->row_offset, A->col_index,
+                                                            (const V *)A->values, x, ldx, alpha, beta, y, ldy);
+    SSPMV_LAUNCH_CHECK();
+    return SSPMV_OK;
+}
+
+template <typename V, int K>
+sspmv_status launch_vector(const sspmv_csr *A, Plan *p, V alpha, const V *x, int64_t ldx, V beta, V *y,
+                           int64_t ldy, sspmv_stream_t s) {
+    int vs = p->vector_lanes;
+    if (vs == 0) {
+        double mean = A->f.num_rows > 0 ? (double)A->f.num_nnzs / (double)A->f.num_rows : 1.0;
+        vs = 2;
+        while (vs < 32 && vs < mean) vs <<= 1;
+    }
+    switch (vs) {
+    case 2: return launch_vector_vs<V, K, 2>(A, alpha, x, ldx, beta, y, ldy, s);
+    case 4: return launch_vector_vs<V, K, 4>(A, alpha, x, ldx, beta, y, ldy, s);
+    case 8: return launch_vector_vs<V, K, 8>(A, alpha, x, ldx, beta, y, ldy, s);
+    case 16: return launch_vector_vs<V, K, 16>(A, alpha, x, ldx, beta, y, ldy, s);
+    default: return launch_vector_vs<V, K, 32>(A, alpha, x, ldx, beta, y, ldy, s);
+    }
+}
+
+template <typename V, int K>
+sspmv_status csr_pass(const sspmv_csr *A, Plan *p, V alpha, const V *x, int64_t ldx, V beta, V *y,
+                      int64_t ldy, sspmv_stream_t s) {
+    if (A->f.kernel_flag == 1) return launch_vector<V, K>(A, p, alpha, x, ldx, beta, y, ldy, s);
+    return launch_merge<V, K>(A, p, alpha, x, ldx, beta, y, ldy, s);
+}
+
+}  // namespace
+
+// Splits k right-hand sides into passes of 8, 4, 2 and 1 columns.
+template <typename V, typename Pass>
+sspmv_status for_rhs_chunks(int32_t k, const V *X, int64_t ldx, V *Y, int64_t ldy, Pass &&pass) {
+    int32_t done = 0;
+    while (done < k) {
+        int32_t left = k - done, step = left >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
+        SSPMV_TRY(pass(step, X + done, Y + done));
+        done += step;
+    }
+    (void)ldx;
+    (void)ldy;
+    return SSPMV_OK;
+}
+
+sspmv_status check_spmm_args(const sspmv_features *f, int32_t k, const void *X, int64_t ldx, const void *Y,
+                             int64_t ldy) {
+    if (k < 1) return fail(SSPMV_INVALID_ARG, "k must be >= 1 (got %d)", k);
+    if (ldx < k || ldy < k) return fail(SSPMV_INVALID_ARG, "ldx/ldy must be >= k");
+    if ((f->num_cols > 0 && !X) || (f->num_rows > 0 && !Y)) return fail(SSPMV_INVALID_ARG, "null x or y");
+    if (!valid_vt(f->value_type)) return fail(SSPMV_INVALID_ARG, "bad value_type");
+    return SSPMV_OK;
+}
+
+sspmv_status spmm_csr_impl(double alpha, const sspmv_csr *A, int32_t k, const void *X, int64_t ldx, double beta,
+                           void *Y, int64_t ldy, sspmv_stream_t s) {
+    if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
+    SSPMV_TRY(check_spmm_args(&A->f, k, X, ldx, Y, ldy));
+    if (A->f.num_rows == 0) return SSPMV_OK;
+    Plan *p = get_plan(&A->f);
+    if (!p) return fail(SSPMV_OUT_OF_MEMORY, "plan allocation failed");
+    return dispatch_value(A->f.value_type, [&](auto tag) -> sspmv_status {
+        using V = decltype(tag);
+        return for_rhs_chunks<V>(k, (const V *)X, ldx, (V *)Y, ldy, [&](int32_t step, const V *xs, V *ys) {
+            const V a = (V)alpha, b = (V)beta;
+            switch (step) {
+            case 8: return csr_pass<V, 8>(A, p, a, xs, ldx, b, ys, ldy, s);
+            case 4: return csr_pass<V, 4>(A, p, a, xs, ldx, b, ys, ldy, s);
+            case 2: return csr_pass<V, 2>(A, p, a, xs, ldx, b, ys, ldy, s);
+            default: return csr_pass<V, 1>(A, p, a, xs, ldx, b, ys, ldy, s);
+            }
+        });
+    });
+}
+
+sspmv_status ensure_merge_plan(Plan *p, int which, int64_t m, int64_t nnz, const int32_t *row_offset,
+                               int32_t value_type, sspmv_stream_t s) {
+    MergePlan &mp = p->merge[which];
+    if (mp.coords) return SSPMV_OK;
+    std::lock_guard<std::mutex> g(plan_mutex());
+    if (mp.coords) return SSPMV_OK;
+    const int tile = which == 0 ? MergeShape<1>::tile : MergeShape<8>::tile;
+    const int64_t tiles = (m + nnz + tile - 1) / tile;
+    const int64_t nt = tiles > 0 ? tiles : 1;
+    MergePlan q;
+    q.tile_items = tile;
+    q.num_tiles = nt;
+    const size_t vs = vsize(value_type);
+    SSPMV_TRY(dalloc(&q.coords, (size_t)nt + 1, s));
+    SSPMV_TRY(dalloc(&q.carry_row, (size_t)nt, s));
+    SSPMV_TRY(dalloc(&q.has_end, (size_t)nt, s));
+    SSPMV_TRY(dalloc((unsigned char **)&q.carry_val, (size_t)nt * kMaxK * vs, s));
+    SSPMV_TRY(dalloc((unsigned char **)&q.head_val, (size_t)nt * kMaxK * vs, s));
+    merge_path_search<<<grid_for(nt + 1, 256), 256, 0, cu(s)>>>(nt, tile, (int)m, (int)nnz, row_offset, q.coords);
+    SSPMV_LAUNCH_CHECK();
+    mp = q;
+    return SSPMV_OK;
+}
+
+}  // namespace sspmv
+
+using namespace sspmv;
+
+extern "C" sspmv_status sspmv_LeSpMV_csr(double alpha, const sspmv_csr *A, const void *x, double beta, void *y,
+                                         sspmv_stream_t stream) {
+    return spmm_csr_impl(alpha, A, 1, x, 1, beta, y, 1, stream);
+}
+
+extern "C" sspmv_status sspmv_spmm_csr(double alpha, const sspmv_csr *A, int32_t k, const void *X, int64_t ldx,
+                                       double beta, void *Y, int64_t ldy, sspmv_stream_t stream) {
+    return spmm_csr_impl(alpha, A, k, X, ldx, beta, Y, ldy, stream);
+}
+
+extern "C" double sspmv_algorithmic_bytes_csr(const sspmv_csr *A, int32_t k, int32_t beta_nonzero) {
+    const double sv = (double)vsize(A->f.value_type);
+    return (double)A->f.num_nnzs * (sv + 4.0) + (double)(A->f.num_rows + 1) * 4.0 +
+           (double)k * (double)A->f.num_cols * sv + (double)k * (double)A->f.num_rows * sv * (beta_nonzero ? 2.0 : 1.0);
+}

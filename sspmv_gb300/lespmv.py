@@ -1,0 +1,214 @@
+"""Reference-facing Python API: LeSpMV's names over the C ABI.
+
+    reference (LeSpMV)                      here
+    CSR_Matrix<I,V> / read_csr_matrix        CSR_Matrix / read_csr_matrix
+    csr_to_<fmt>(csr, params...)             csr_to_<fmt>(csr, params...)
+    LeSpMV_<fmt>(alpha, A, x, beta, y)       LeSpMV_<fmt>(alpha, A, x, beta, y)
+    delete_host_matrix(A)                    A.delete() (or garbage collection)
+
+Matrices live on the GPU; x and y are CUDA tensors (torch) or raw device
+pointers.  Calls are ordered on the current torch stream unless a stream is
+given.  Errors raise SSPMVError carrying the library's status.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import Csr, F32, F64, SSPMVError, call, lib
+from .synth import HostCSR
+
+RowMajor, ColMajor = _lib.ROW_MAJOR, _lib.COL_MAJOR
+
+
+def _stream(stream) -> C.c_void_p:
+    if stream is None:
+        import torch
+        return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if hasattr(stream, "cuda_stream"):
+        return C.c_void_p(stream.cuda_stream)
+    return C.c_void_p(int(stream))
+
+
+def _dptr(t) -> C.c_void_p:
+    if t is None:
+        return C.c_void_p(None)
+    if hasattr(t, "data_ptr"):
+        return C.c_void_p(t.data_ptr())
+    return C.c_void_p(int(t))
+
+
+def _vt(dtype) -> int:
+    return F64 if np.dtype(dtype) == np.float64 else F32
+
+
+class Matrix:
+    """Base of the format wrappers: owns one C struct and frees it."""
+    fmt = ""
+    struct = None
+
+    def __init__(self, s):
+        self.s = s
+        self._alive = True
+
+    @property
+    def num_rows(self) -> int:
+        return int(self.s.f.num_rows)
+
+    @property
+    def num_cols(self) -> int:
+        return int(self.s.f.num_cols)
+
+    @property
+    def num_nnzs(self) -> int:
+        return int(self.s.f.num_nnzs)
+
+    @property
+    def dtype(self):
+        return np.float64 if self.s.f.value_type == F64 else np.float32
+
+    @property
+    def kernel_flag(self) -> int:
+        return int(self.s.f.kernel_flag)
+
+    @kernel_flag.setter
+    def kernel_flag(self, v: int) -> None:
+        self.s.f.kernel_flag = int(v)
+
+    def ref(self):
+        return C.byref(self.s)
+
+    def delete(self) -> None:
+        if self._alive:
+            self._alive = False
+            getattr(lib, f"sspmv_delete_{self.fmt}")(C.byref(self.s))
+
+    def __del__(self):
+        try:
+            self.delete()
+        except Exception:
+            pass
+
+    def algorithmic_bytes(self, k: int = 1, beta_nonzero: bool = False) -> float:
+        return float(getattr(lib, f"sspmv_algorithmic_bytes_{self.fmt}")(self.ref(), k, int(beta_nonzero)))
+
+
+class CSR_Matrix(Matrix):
+    fmt = "csr"
+
+    def export(self, stream=None) -> dict:
+        rp = np.empty(self.num_rows + 1, np.int32)
+        col = np.empty(self.num_nnzs, np.int32)
+        val = np.empty(self.num_nnzs, self.dtype)
+        call("sspmv_csr_export", self.ref(), rp.ctypes.data_as(C.c_void_p), col.ctypes.data_as(C.c_void_p),
+             val.ctypes.data_as(C.c_void_p), _stream(stream))
+        return {"row_offset": rp, "col": col, "val": val}
+
+
+def csr_from_host(A: HostCSR, stream=None) -> CSR_Matrix:
+    """Uploads a host CSR (the reference's CSR_Matrix) to the device."""
+    s = Csr()
+    vals = np.ascontiguousarray(A.values)
+    call("sspmv_csr_create", C.byref(s), _vt(vals.dtype), A.num_rows, A.num_cols, A.nnz,
+         A.row_offset.ctypes.data_as(C.c_void_p), A.col_index.ctypes.data_as(C.c_void_p),
+         vals.ctypes.data_as(C.c_void_p), 1, _stream(stream))
+    return CSR_Matrix(s)
+
+
+def read_csr_matrix(path: str, precision: int = 64) -> HostCSR:
+    """read_csr_matrix (utils/sparse_io.cpp:180-204) on the host."""
+    vt = F64 if precision == 64 else F32
+    m, n, nnz = C.c_int64(), C.c_int64(), C.c_int64()
+    call("sspmv_read_mtx", str(path).encode(), vt, C.byref(m), C.byref(n), C.byref(nnz), None, None, None)
+    rp = np.empty(m.value + 1, np.int32)
+    col = np.empty(nnz.value, np.int32)
+    val = np.empty(nnz.value, np.float64 if vt == F64 else np.float32)
+    call("sspmv_read_mtx", str(path).encode(), vt, C.byref(m), C.byref(n), C.byref(nnz),
+         rp.ctypes.data_as(C.c_void_p), col.ctypes.data_as(C.c_void_p), val.ctypes.data_as(C.c_void_p))
+    return HostCSR(int(m.value), int(n.value), rp, col, val)
+
+
+def write_mtx(path: str, A: HostCSR) -> None:
+    vals = np.ascontiguousarray(A.values, dtype=np.float64)
+    call("sspmv_write_mtx", str(path).encode(), A.num_rows, A.num_cols, A.row_offset.ctypes.data_as(C.c_void_p),
+         A.col_index.ctypes.data_as(C.c_void_p), vals.ctypes.data_as(C.c_void_p))
+
+
+def LeSpMV(alpha: float, A: Matrix, x, beta: float, y, stream=None) -> None:
+    """y = alpha*A*x + beta*y for any format (LeSpMV_<fmt>)."""
+    call(f"sspmv_LeSpMV_{A.fmt}", float(alpha), A.ref(), _dptr(x), float(beta), _dptr(y), _stream(stream))
+
+
+def spmm(alpha: float, A: Matrix, X, beta: float, Y, k: int | None = None, ldx: int | None = None,
+         ldy: int | None = None, stream=None) -> None:
+    """Y = alpha*A*X + beta*Y, X row-major num_cols x k, Y num_rows x k."""
+    if k is None:
+        k = int(X.shape[1]) if hasattr(X, "shape") and len(X.shape) == 2 else 1
+    ldx = ldx or (int(X.stride(0)) if hasattr(X, "stride") and len(X.shape) == 2 else k)
+    ldy = ldy or (int(Y.stride(0)) if hasattr(Y, "stride") and len(Y.shape) == 2 else k)
+    call(f"sspmv_spmm_{A.fmt}", float(alpha), A.ref(), int(k), _dptr(X), int(ldx), float(beta), _dptr(Y), int(ldy),
+         _stream(stream))
+
+
+def LeSpMV_csr(alpha, A: CSR_Matrix, x, beta, y, stream=None) -> None:
+    LeSpMV(alpha, A, x, beta, y, stream)
+
+
+# Formats the library builds, in benchmark order.
+FORMATS = ["csr"]
+# Formats the smoke check converts from CSR (besides CSR itself).
+SMOKE_FORMATS: list[str] = []
+
+
+def bsr_block_for(A: HostCSR) -> tuple[int, int]:
+    """Block shape used for a host matrix when none is given: 4x4."""
+    return 4, 4
+
+
+def feasible_host(fmt: str, A: HostCSR) -> tuple[bool, str]:
+    """Whether `fmt` is worth building for A (padding within 4x the CSR size,
+    DIA within the reference's 10240-diagonal limit)."""
+    if fmt in ("csr", "coo", "csr5", "sell", "sell_c_sigma", "sell_c_R"):
+        return True, ""
+    m, nnz = A.num_rows, max(A.nnz, 1)
+    lens = np.diff(A.row_offset)
+    if fmt == "ell":
+        w = int(lens.max()) if m else 0
+        return (m * w <= 4 * nnz, f"ELL width {w} pads {m * w / nnz:.1f}x")
+    if fmt == "dia":
+        rows = np.repeat(np.arange(m, dtype=np.int64), lens)
+        nd = len(np.unique(A.col_index.astype(np.int64) - rows))
+        return (nd <= 10240, f"{nd} diagonals > 10240")
+    if fmt == "bsr":
+        r, c = bsr_block_for(A)
+        rows = np.repeat(np.arange(m, dtype=np.int64), lens) // r
+        keys = rows * ((A.num_cols + c - 1) // c) + A.col_index // c
+        nnzb = len(np.unique(keys))
+        return (nnzb * r * c <= 4 * nnz, f"BSR {r}x{c} fill {nnzb * r * c / nnz:.1f}x")
+    return False, "unknown format"
+
+
+def build_format(csr: CSR_Matrix, fmt: str, A: HostCSR | None = None):
+    """Converts a device CSR to `fmt`; returns (matrix, None) or (None, why)."""
+    if A is not None:
+        ok, why = feasible_host(fmt, A)
+        if not ok:
+            return None, why
+    if fmt == "csr":
+        return csr, None
+    fn = globals().get(f"csr_to_{fmt}")
+    if fn is None:
+        return None, "not built"
+    try:
+        if fmt == "bsr" and A is not None:
+            r, c = bsr_block_for(A)
+            return fn(csr, r, c), None
+        return fn(csr), None
+    except SSPMVError as e:
+        return None, str(e)
+
+
+__all__ = ["CSR_Matrix", "csr_from_host", "read_csr_matrix", "write_mtx", "LeSpMV", "LeSpMV_csr", "spmm",
+           "RowMajor", "ColMajor", "SSPMVError"]

@@ -1,0 +1,96 @@
+"""CSR SpMV / SpMM on the GPU against the reference's own results (golden
+fixtures) and the FP64 oracle, through the C ABI.
+
+Tolerance (per row, FP64 and FP32): |y_i - y_ref_i| <= 8*nnz_i*eps*|alpha|*
+sum_j|a_ij x_j| + 2*eps*|beta*y0_i|, y_ref the FP64 CSR result on the same
+(possibly FP32-rounded) inputs."""
+import numpy as np
+import pytest
+
+from golden_util import ALPHA, BETA, files, load
+from gpu_util import to_dev, to_host
+from oracle import tolerance_ok
+
+pytestmark = pytest.mark.gpu
+
+CASES = files()
+
+
+def _csr(A):
+    from sspmv_gb300.lespmv import csr_from_host
+    return csr_from_host(A)
+
+
+@pytest.mark.parametrize("flag", [0, 1])
+@pytest.mark.parametrize("path", CASES, ids=[p.stem for p in CASES])
+def test_csr_golden(path, flag, oracle_lib):
+    from sspmv_gb300.lespmv import LeSpMV_csr
+    z, meta, A = load(path)
+    dt = A.values.dtype
+    x, y0 = z["x"], z["y0"]
+    M = _csr(A)
+    M.kernel_flag = flag
+    y = to_dev(y0)
+    LeSpMV_csr(ALPHA, M, to_dev(x), BETA, y)
+    yg = to_host(y)
+    y64, absum = oracle_lib.spmm_ref(A, x, ALPHA, BETA, y0)
+    ok, mx, med = tolerance_ok(yg, y64, absum, np.diff(A.row_offset), dt, ALPHA, BETA, y0)
+    assert ok, f"max normalised error {mx}"
+    assert oracle_lib.max_rel_error(yg, z["y_csr_2"]) < 5 * np.sqrt(np.finfo(dt).eps)
+
+
+FAMILIES = {
+    "powerlaw": lambda s: s.powerlaw(60000, 1.8, 16.0, 50000, 0.02),
+    "uniform": lambda s: s.uniform(50000, 32, 0.01),
+    "laplacian": lambda s: s.laplacian2d(300),
+    "banded": lambda s: s.banded(40000),
+    "block": lambda s: s.block(40000, 4, 9000),
+}
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
+@pytest.mark.parametrize("fam", list(FAMILIES))
+@pytest.mark.parametrize("k", [1, 2, 3, 8])
+def test_csr_spmm_families(fam, k, dt, oracle_lib):
+    from sspmv_gb300 import synth
+    from sspmv_gb300.lespmv import spmm
+    A = synth.generate(FAMILIES[fam](synth), 2, dt)
+    X = synth.vector(A.num_cols, 0, dt, k).reshape(A.num_cols, k)
+    Y0 = synth.vector(A.num_rows, 7, dt, k).reshape(A.num_rows, k)
+    M = _csr(A)
+    for flag in (0, 1):
+        M.kernel_flag = flag
+        Y = to_dev(Y0)
+        spmm(ALPHA, M, to_dev(X), BETA, Y)
+        Yg = to_host(Y)
+        y64, absum = oracle_lib.spmm_ref(A, X, ALPHA, BETA, Y0)
+        ok, mx, med = tolerance_ok(Yg, y64, absum, np.diff(A.row_offset), dt, ALPHA, BETA, Y0)
+        assert ok, f"{fam} k={k} flag={flag}: max normalised error {mx}"
+
+
+def test_csr_beta_zero_ignores_nan_y(oracle_lib):
+    from sspmv_gb300 import synth
+    from sspmv_gb300.lespmv import LeSpMV_csr
+    A = synth.generate(synth.powerlaw(20000, 1.8, 16, 20000, 0.05), 4)
+    x = synth.vector(A.num_cols, 0)
+    M = _csr(A)
+    y = to_dev(np.full(A.num_rows, np.nan))
+    LeSpMV_csr(1.0, M, to_dev(x), 0.0, y)
+    yg = to_host(y)
+    y64, absum = oracle_lib.spmm_ref(A, x, 1.0, 0.0)
+    ok, mx, _ = tolerance_ok(yg, y64, absum, np.diff(A.row_offset), np.float64)
+    assert ok and np.isfinite(yg).all()
+
+
+def test_csr_deterministic():
+    from sspmv_gb300 import synth
+    from sspmv_gb300.lespmv import LeSpMV_csr
+    A = synth.generate(synth.powerlaw(100000, 1.8, 16, 50000), 6)
+    x = to_dev(synth.vector(A.num_cols, 0))
+    M = _csr(A)
+    outs = []
+    for _ in range(3):
+        y = to_dev(np.zeros(A.num_rows))
+        LeSpMV_csr(1.0, M, x, 0.0, y)
+        outs.append(to_host(y))
+    assert all(np.array_equal(outs[0], o) for o in outs[1:])
