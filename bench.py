@@ -50,6 +50,7 @@ def parse_args():
     ap.add_argument("--dtypes", default=",".join(DTYPES))
     ap.add_argument("--scale", type=float, default=1.0, help="row-count scale (testing only)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (library defaults)")
     return ap.parse_args()
 
 
@@ -164,6 +165,18 @@ def run_gpu(args, rank, world):
                               "rows": A.num_rows, "cols": A.num_cols})
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
+    if not args.no_tune:
+        from sspmv_gb300 import autotune
+        seen = set()
+        for c in cases:
+            if id(c["M"]) in seen:  # CSR is shared by a family's formats
+                continue
+            seen.add(id(c["M"]))
+            res = autotune.tune_format(c["M"], c["x"], c["y"])
+            c["tuned"] = res["best"] if res else None
+    for c in cases:
+        c.setdefault("tuned", None)
+        c["kernel"] = {"kernel_flag": c["M"].kernel_flag}
 
     def one_step(record):
         for c in cases:
@@ -208,7 +221,8 @@ def run_gpu(args, rank, world):
         total_bytes += c["bytes"] * len(ms)
         per_case.append({"family": c["fam"], "format": c["fmt"], "dtype": c["dt"], "ms": round(avg, 5),
                          "GBps": round(c["bytes"] / avg / 1e6, 1),
-                         "GFLOPs": round(2.0 * c["nnz"] / avg / 1e6, 1)})
+                         "GFLOPs": round(2.0 * c["nnz"] / avg / 1e6, 1),
+                         "kernel": c["tuned"] or c["kernel"]})
     step_ms = total_ms / args.steps
     step_ms = _max_over_ranks(step_ms, world)
     value = total_bytes / args.steps * world / (step_ms * 1e6)

@@ -92,12 +92,80 @@ typedef struct {
     void *values;
 } sspmv_csr;
 
+/* ELL_Matrix (include/sparse_format.h:192-205).  Device storage is always
+ * column-major (slot k of row i at k*num_rows + i, padding col -1 / value 0);
+ * `ld` records the layout the reference would hold, used by the export. */
+typedef struct {
+    sspmv_features f;
+    int32_t ld;
+    int32_t max_row_width;
+    int32_t min_row_width;
+    int32_t *col_index;
+    void *values;
+} sspmv_ell;
+
+/* S_ELL_Matrix (include/sparse_format.h:214-238).  The reference keeps one
+ * allocation per chunk (T**); here all chunks share one slab and chunk c
+ * starts at slot chunk_ptr[c].  Inside a chunk storage is slot-major (slot k
+ * of the chunk's row r at chunk_ptr[c] + k*sliceWidth + r), so C consecutive
+ * rows are read together; the export returns the reference's row-major
+ * chunks. */
+typedef struct {
+    sspmv_features f;
+    int32_t sliceWidth; /* C rows per chunk */
+    int32_t chunk_num;
+    int32_t alignment;
+    int32_t *row_width; /* [chunk_num], multiples of alignment */
+    int64_t *chunk_ptr; /* [chunk_num + 1] */
+    int64_t total_slots;
+    int32_t *col_index;
+    void *values;
+} sspmv_s_ell;
+
+/* SELL_C_Sigma_Matrix (include/sparse_format.h:245-270); chunk storage as
+ * sspmv_s_ell.  reorder[i] is the original row stored at position i. */
+typedef struct {
+    sspmv_features f;
+    int32_t sliceWidth_Sigma;
+    int32_t chunkWidth_C;
+    int32_t sliceNum;
+    int32_t chunkNum;
+    int32_t validchunkNum;
+    int32_t chunk_num_per_slice;
+    int32_t alignment;
+    int32_t *reorder;   /* [num_rows] */
+    int32_t *chunk_len; /* [validchunkNum] */
+    int64_t *chunk_ptr; /* [validchunkNum + 1] */
+    int64_t total_slots;
+    int32_t *col_index;
+    void *values;
+} sspmv_sell_c_sigma;
+
+/* SELL_C_R_Matrix (include/sparse_format.h:275-295): SELL-c-sigma with one
+ * slice holding every row. */
+typedef struct {
+    sspmv_features f;
+    int32_t chunkWidth_C;
+    int32_t validchunkNum;
+    int32_t alignment;
+    int32_t *reorder;
+    int32_t *chunk_len;
+    int64_t *chunk_ptr;
+    int64_t total_slots;
+    int32_t *col_index;
+    void *values;
+} sspmv_sell_c_R;
+
 /* ---------------- status / memory ---------------- */
 const char *sspmv_status_string(sspmv_status s);
 const char *sspmv_last_error(void);
 const char *sspmv_version(void);
 /* Number of kernels this library has launched in the process so far. */
 int64_t sspmv_launch_count(void);
+/* Selects the SpMV kernel of a matrix (pass &A->f): kernel_flag as in each
+ * format's LeSpMV entry, param a kernel parameter (CSR vector kernel: lanes
+ * per row 2..32; 0 lets the library choose).  Used by the autotuner. */
+sspmv_status sspmv_set_kernel(sspmv_features *f, int32_t kernel_flag, int32_t param);
 
 /* ---------------- CSR creation ---------------- */
 /* Device CSR from arrays.  from_host != 0: copies host arrays to library-
@@ -122,9 +190,71 @@ sspmv_status sspmv_LeSpMV_csr(double alpha, const sspmv_csr *A, const void *x, d
 sspmv_status sspmv_spmm_csr(double alpha, const sspmv_csr *A, int32_t k, const void *X, int64_t ldx,
                             double beta, void *Y, int64_t ldy, sspmv_stream_t stream);
 
+/* ---------------- ELL ---------------- */
+/* csr_to_ell (include/sparse_conversion.h:187-248) */
+sspmv_status sspmv_csr_to_ell(const sspmv_csr *csr, int32_t ld, sspmv_ell *out, sspmv_stream_t stream);
+/* LeSpMV_ell (src/spmv_ell.cpp:225-247): one thread per row over the
+ * column-major slots, stopping at the row's first padding slot. */
+sspmv_status sspmv_LeSpMV_ell(double alpha, const sspmv_ell *A, const void *x, double beta, void *y,
+                              sspmv_stream_t stream);
+sspmv_status sspmv_spmm_ell(double alpha, const sspmv_ell *A, int32_t k, const void *X, int64_t ldx,
+                            double beta, void *Y, int64_t ldy, sspmv_stream_t stream);
+/* col_index / values: num_rows*max_row_width each, in A->ld layout. */
+sspmv_status sspmv_ell_export(const sspmv_ell *A, int32_t *col_index, void *values, sspmv_stream_t stream);
+sspmv_status sspmv_delete_ell(sspmv_ell *A);
+
+/* ---------------- S-ELL ---------------- */
+/* csr_to_sell (include/sparse_conversion.h:258-334); chunkwidth / alignment
+ * 0 = reference defaults (4, 64/sizeof(value)). */
+sspmv_status sspmv_csr_to_sell(const sspmv_csr *csr, int32_t chunkwidth, int32_t alignment, sspmv_s_ell *out,
+                               sspmv_stream_t stream);
+/* LeSpMV_sell (src/spmv_s_ell.cpp:203-224) */
+sspmv_status sspmv_LeSpMV_sell(double alpha, const sspmv_s_ell *A, const void *x, double beta, void *y,
+                               sspmv_stream_t stream);
+sspmv_status sspmv_spmm_sell(double alpha, const sspmv_s_ell *A, int32_t k, const void *X, int64_t ldx,
+                             double beta, void *Y, int64_t ldy, sspmv_stream_t stream);
+/* row_width: chunk_num; col_index / values: total_slots, chunks in order,
+ * row-major inside a chunk (the reference's layout). */
+sspmv_status sspmv_sell_export(const sspmv_s_ell *A, int32_t *row_width, int32_t *col_index, void *values,
+                               sspmv_stream_t stream);
+sspmv_status sspmv_delete_sell(sspmv_s_ell *A);
+
+/* ---------------- SELL-c-sigma ---------------- */
+/* csr_to_sell_c_sigma (include/sparse_conversion.h:337-479): rows sorted by
+ * nonzero count, descending, inside each sigma-slice (ties: larger row
+ * first).  slicewidth % chunkwidth != 0 -> SSPMV_INVALID_ARG (the reference
+ * exits).  0 = defaults (16384, 4, 64/sizeof(value)). */
+sspmv_status sspmv_csr_to_sell_c_sigma(const sspmv_csr *csr, int32_t slicewidth, int32_t chunkwidth,
+                                       int32_t alignment, sspmv_sell_c_sigma *out, sspmv_stream_t stream);
+/* LeSpMV_sell_c_sigma (src/spmv_sell_c_sigma.cpp:190-211) */
+sspmv_status sspmv_LeSpMV_sell_c_sigma(double alpha, const sspmv_sell_c_sigma *A, const void *x, double beta,
+                                       void *y, sspmv_stream_t stream);
+sspmv_status sspmv_spmm_sell_c_sigma(double alpha, const sspmv_sell_c_sigma *A, int32_t k, const void *X,
+                                     int64_t ldx, double beta, void *Y, int64_t ldy, sspmv_stream_t stream);
+sspmv_status sspmv_sell_c_sigma_export(const sspmv_sell_c_sigma *A, int32_t *reorder, int32_t *chunk_len,
+                                       int32_t *col_index, void *values, sspmv_stream_t stream);
+sspmv_status sspmv_delete_sell_c_sigma(sspmv_sell_c_sigma *A);
+
+/* ---------------- SELL-c-R ---------------- */
+/* csr_to_sell_c_R (include/sparse_conversion.h:483-598) */
+sspmv_status sspmv_csr_to_sell_c_R(const sspmv_csr *csr, int32_t chunkwidth, int32_t alignment,
+                                   sspmv_sell_c_R *out, sspmv_stream_t stream);
+/* LeSpMV_sell_c_R (src/spmv_sell_c_R.cpp:190-211) */
+sspmv_status sspmv_LeSpMV_sell_c_R(double alpha, const sspmv_sell_c_R *A, const void *x, double beta, void *y,
+                                   sspmv_stream_t stream);
+sspmv_status sspmv_spmm_sell_c_R(double alpha, const sspmv_sell_c_R *A, int32_t k, const void *X, int64_t ldx,
+                                 double beta, void *Y, int64_t ldy, sspmv_stream_t stream);
+sspmv_status sspmv_sell_c_R_export(const sspmv_sell_c_R *A, int32_t *reorder, int32_t *chunk_len,
+                                   int32_t *col_index, void *values, sspmv_stream_t stream);
+sspmv_status sspmv_delete_sell_c_R(sspmv_sell_c_R *A);
+
 /* Algorithmic bytes of one SpMV with k right-hand sides: structural bytes of
  * the format (padding excluded) + x once + y once (twice when beta != 0). */
 double sspmv_algorithmic_bytes_csr(const sspmv_csr *A, int32_t k, int32_t beta_nonzero);
+double sspmv_algorithmic_bytes_ell(const sspmv_ell *A, int32_t k, int32_t beta_nonzero);
+double sspmv_algorithmic_bytes_sell(const sspmv_s_ell *A, int32_t k, int32_t beta_nonzero);
+double sspmv_algorithmic_bytes_sell_c_sigma(const sspmv_sell_c_sigma *A, int32_t k, int32_t beta_nonzero);
+double sspmv_algorithmic_bytes_sell_c_R(const sspmv_sell_c_R *A, int32_t k, int32_t beta_nonzero);
 
 /* ---------------- host utilities ---------------- */
 /* Matrix Market reader (utils/sparse_io.cpp:27-204: coordinate format,

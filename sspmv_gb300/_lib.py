@@ -43,6 +43,34 @@ class Csr(C.Structure):
     _fields_ = [("f", Features), ("row_offset", P32), ("col_index", P32), ("values", C.c_void_p)]
 
 
+P64 = C.POINTER(C.c_int64)
+
+
+class Ell(C.Structure):
+    _fields_ = [("f", Features), ("ld", C.c_int32), ("max_row_width", C.c_int32), ("min_row_width", C.c_int32),
+                ("col_index", P32), ("values", C.c_void_p)]
+
+
+class SEll(C.Structure):
+    _fields_ = [("f", Features), ("sliceWidth", C.c_int32), ("chunk_num", C.c_int32), ("alignment", C.c_int32),
+                ("row_width", P32), ("chunk_ptr", P64), ("total_slots", C.c_int64), ("col_index", P32),
+                ("values", C.c_void_p)]
+
+
+class SellCSigma(C.Structure):
+    _fields_ = [("f", Features), ("sliceWidth_Sigma", C.c_int32), ("chunkWidth_C", C.c_int32),
+                ("sliceNum", C.c_int32), ("chunkNum", C.c_int32), ("validchunkNum", C.c_int32),
+                ("chunk_num_per_slice", C.c_int32), ("alignment", C.c_int32), ("reorder", P32),
+                ("chunk_len", P32), ("chunk_ptr", P64), ("total_slots", C.c_int64), ("col_index", P32),
+                ("values", C.c_void_p)]
+
+
+class SellCR(C.Structure):
+    _fields_ = [("f", Features), ("chunkWidth_C", C.c_int32), ("validchunkNum", C.c_int32),
+                ("alignment", C.c_int32), ("reorder", P32), ("chunk_len", P32), ("chunk_ptr", P64),
+                ("total_slots", C.c_int64), ("col_index", P32), ("values", C.c_void_p)]
+
+
 class SynthParams(C.Structure):
     _fields_ = [("family", C.c_int32), ("num_offsets", C.c_int32), ("num_rows", C.c_int64),
                 ("num_cols", C.c_int64), ("grid", C.c_int64), ("offsets", C.c_int64 * 32),
@@ -71,6 +99,7 @@ _SIGS = {
     "sspmv_last_error": (C.c_char_p, []),
     "sspmv_version": (C.c_char_p, []),
     "sspmv_launch_count": (_i64, []),
+    "sspmv_set_kernel": (_st, [C.POINTER(Features), _i32, _i32]),
     "sspmv_csr_create": (_st, [C.POINTER(Csr), _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp]),
     "sspmv_csr_wrap": (_st, [C.POINTER(Csr), _i32, _i64, _i64, _i64, _vp, _vp, _vp]),
     "sspmv_csr_export": (_st, [C.POINTER(Csr), _vp, _vp, _vp, _vp]),
@@ -93,6 +122,25 @@ def register(name: str, restype, argtypes) -> None:
     fn.restype = restype
     fn.argtypes = argtypes
 
+
+def _format_sigs(fmt: str, struct, convert_args, export_args):
+    P = C.POINTER(struct)
+    sigs = {
+        f"sspmv_LeSpMV_{fmt}": (_st, [_d, P, _vp, _d, _vp, _vp]),
+        f"sspmv_spmm_{fmt}": (_st, [_d, P, _i32, _vp, _i64, _d, _vp, _i64, _vp]),
+        f"sspmv_delete_{fmt}": (_st, [P]),
+        f"sspmv_algorithmic_bytes_{fmt}": (_d, [P, _i32, _i32]),
+        f"sspmv_{fmt}_export": (_st, [P, *export_args, _vp]),
+    }
+    if convert_args is not None:
+        sigs[f"sspmv_csr_to_{fmt}"] = (_st, [C.POINTER(Csr), *convert_args, P, _vp])
+    return sigs
+
+
+_SIGS.update(_format_sigs("ell", Ell, [_i32], [_vp, _vp]))
+_SIGS.update(_format_sigs("sell", SEll, [_i32, _i32], [_vp, _vp, _vp]))
+_SIGS.update(_format_sigs("sell_c_sigma", SellCSigma, [_i32, _i32, _i32], [_vp, _vp, _vp, _vp]))
+_SIGS.update(_format_sigs("sell_c_R", SellCR, [_i32, _i32], [_vp, _vp, _vp, _vp]))
 
 for _n, (_r, _a) in _SIGS.items():
     register(_n, _r, _a)

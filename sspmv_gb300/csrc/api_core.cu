@@ -98,12 +98,33 @@ extern "C" const char *sspmv_version(void) { return "sspmv-gb300 0.1 (sm_103a)";
 
 extern "C" int64_t sspmv_launch_count(void) { return (int64_t)g_launches.load(); }
 
+extern "C" sspmv_status sspmv_set_kernel(sspmv_features *f, int32_t kernel_flag, int32_t param) {
+    if (!f) return fail(SSPMV_INVALID_ARG, "null matrix");
+    if (kernel_flag < 0 || param < 0) return fail(SSPMV_INVALID_ARG, "negative kernel_flag or param");
+    Plan *p = get_plan(f);
+    if (!p) return fail(SSPMV_OUT_OF_MEMORY, "plan allocation failed");
+    f->kernel_flag = kernel_flag;
+    p->param = param;
+    return SSPMV_OK;
+}
+
 extern "C" sspmv_status sspmv_csr_create(sspmv_csr *out, int32_t vt, int64_t m, int64_t n, int64_t nnz,
                                          const int32_t *row_offset, const int32_t *col_index, const void *values,
                                          int32_t from_host, sspmv_stream_t s) {
     if (!out) return fail(SSPMV_INVALID_ARG, "null output");
     SSPMV_TRY(check_dims(vt, m, n, nnz));
     if (!row_offset || (nnz > 0 && (!col_index || !values))) return fail(SSPMV_INVALID_ARG, "null array");
+    if (from_host) {
+        // Kernels index x by col_index and y by row: reject malformed input
+        // before it reaches the device.
+        if (row_offset[0] != 0 || row_offset[m] != nnz) return fail(SSPMV_INVALID_ARG, "row_offset[0] != 0 or row_offset[m] != nnz");
+        long long bad = 0;
+#pragma omp parallel for reduction(+ : bad)
+        for (int64_t i = 0; i < m; i++) bad += row_offset[i + 1] < row_offset[i];
+#pragma omp parallel for reduction(+ : bad)
+        for (int64_t j = 0; j < nnz; j++) bad += (col_index[j] < 0 || col_index[j] >= n);
+        if (bad) return fail(SSPMV_INVALID_ARG, "row_offset not monotone or column index out of [0, num_cols)");
+    }
     sspmv_csr A;
     init_features(&A.f, vt, m, n, nnz, 1);
     A.row_offset = nullptr;

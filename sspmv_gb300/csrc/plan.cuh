@@ -28,7 +28,7 @@ constexpr int kMaxK = 8;  // right-hand sides handled per pass
 struct Plan {
     int kind = 0;
     MergePlan merge[2];     // [0]: tile for k <= 4, [1]: tile for k == 8
-    int vector_lanes = 0;   // CSR vector kernel lanes per row (0 = not chosen)
+    int param = 0;          // kernel parameter set by sspmv_set_kernel (0 = library choice)
     void *extra[8] = {nullptr};  // format-specific device buffers
     int64_t extra_i[8] = {0};
 };

@@ -1,0 +1,595 @@
+// sliced.cu -- ELL, S-ELL, SELL-c-sigma and SELL-c-R on sm_103a: GPU
+// converters from CSR, SpMV / SpMM kernels, export to the reference layout.
+//
+// All four share one device layout: a slab of chunks, chunk c holding C rows
+// in slot-major order (slot k of the chunk's row r at chunk_ptr[c] + k*C + r,
+// padding col -1 / value 0 after each row's last nonzero).  ELL is the case
+// of one chunk of C = num_rows rows (the reference's column-major ELL).
+// A thread owns one (stored) row: the C threads of a chunk read C consecutive
+// slots per step, and a warp covers 32/C chunks.  A row stops at its first
+// padding slot, so padding costs at most one partially used sector per row
+// instead of being streamed.  SELL variants write y through `reorder`.
+//
+// Converters (bit-exact logical content vs the reference):
+//   ELL          include/sparse_conversion.h:187-248
+//   S-ELL        include/sparse_conversion.h:258-334
+//   SELL-c-sigma include/sparse_conversion.h:337-479 (sort: nnz desc, row desc)
+//   SELL-c-R     include/sparse_conversion.h:483-598
+// The per-slice sort is a stable LSD radix sort of keys
+// slice*(maxlen+1) + (maxlen - len) over rows fed in descending row order.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "plan.cuh"
+#include "primitives.cuh"
+#include "spmv_common.cuh"
+
+namespace sspmv {
+sspmv_status check_dims(int32_t vt, int64_t m, int64_t n, int64_t nnz);
+void init_features(sspmv_features *f, int32_t vt, int64_t m, int64_t n, int64_t nnz, int32_t owns);
+}  // namespace sspmv
+
+using namespace sspmv;
+
+namespace {
+
+constexpr int kBlock = 256;
+
+// ------------------------------------------------------------------ SpMV --
+template <typename V, int K>
+__global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
+    int m, int C, const int64_t *__restrict__ chunk_ptr, const int32_t *__restrict__ reorder,
+    const int32_t *__restrict__ col, const V *__restrict__ val, const V *__restrict__ x, int64_t ldx, V alpha,
+    V beta, V *__restrict__ y, int64_t ldy) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = i / C;
+        const int r = (int)(i - c * C);
+        const int64_t base = ld_stream(chunk_ptr + c);
+        const int64_t w = (ld_stream(chunk_ptr + c + 1) - base) / C;
+        const int32_t *cp = col + base + r;
+        const V *vp = val + base + r;
+        V s[K];
+#pragma unroll
+        for (int q = 0; q < K; q++) s[q] = V(0);
+        int64_t k = 0;
+        for (; k + 4 <= w; k += 4) {
+            int cc[4];
+            V aa[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                cc[u] = ld_stream(cp + (k + u) * C);
+                aa[u] = ld_stream(vp + (k + u) * C);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (cc[u] >= 0) {
+#pragma unroll
+                    for (int q = 0; q < K; q++) s[q] += aa[u] * ld_x(x + (int64_t)cc[u] * ldx + q);
+                }
+            if (cc[3] < 0) break;  // padding is a suffix of the row
+        }
+        if (k + 4 > w) {
+            for (; k < w; k++) {
+                const int cc = ld_stream(cp + k * C);
+                if (cc < 0) break;
+                const V aa = ld_stream(vp + k * C);
+#pragma unroll
+                for (int q = 0; q < K; q++) s[q] += aa * ld_x(x + (int64_t)cc * ldx + q);
+            }
+        }
+        const int64_t row = reorder ? (int64_t)ld_stream(reorder + i) : i;
+        V *yp = y + row * ldy;
+#pragma unroll
+        for (int q = 0; q < K; q++) yp[q] = axpby(alpha, s[q], beta, yp + q);
+    }
+}
+
+struct SlicedView {
+    int64_t m;
+    int32_t C;
+    const int64_t *chunk_ptr;
+    const int32_t *reorder;
+    const int32_t *col;
+    const void *val;
+};
+
+template <typename V, int K>
+sspmv_status launch_sliced(const SlicedView &v, V alpha, const V *x, int64_t ldx, V beta, V *y, int64_t ldy,
+                           sspmv_stream_t s) {
+    const unsigned grid = grid_for(v.m, kBlock, (int64_t)num_sms() * 16);
+    sliced_spmv_kernel<V, K><<<grid, kBlock, 0, cu(s)>>>((int)v.m, v.C, v.chunk_ptr, v.reorder, v.col,
+                                                         (const V *)v.val, x, ldx, alpha, beta, y, ldy);
+    SSPMV_LAUNCH_CHECK();
+    return SSPMV_OK;
+}
+
+sspmv_status spmm_sliced(const sspmv_features *f, const SlicedView &v, double alpha, int32_t k, const void *X,
+                         int64_t ldx, double beta, void *Y, int64_t ldy, sspmv_stream_t s) {
+    SSPMV_TRY(check_spmm_args(f, k, X, ldx, Y, ldy));
+    if (v.m == 0) return SSPMV_OK;
+    return dispatch_value(f->value_type, [&](auto tag) -> sspmv_status {
+        using V = decltype(tag);
+        return for_rhs_chunks<V>(k, (const V *)X, (V *)Y, [&](int32_t step, const V *xs, V *ys) {
+            const V a = (V)alpha, b = (V)beta;
+            switch (step) {
+            case 8: return launch_sliced<V, 8>(v, a, xs, ldx, b, ys, ldy, s);
+            case 4: return launch_sliced<V, 4>(v, a, xs, ldx, b, ys, ldy, s);
+            case 2: return launch_sliced<V, 2>(v, a, xs, ldx, b, ys, ldy, s);
+            default: return launch_sliced<V, 1>(v, a, xs, ldx, b, ys, ldy, s);
+            }
+        });
+    });
+}
+
+// ------------------------------------------------------------ converters --
+// keys for the slice sort: position p holds row m-1-p (descending input order)
+__global__ void sell_sort_keys(int64_t m, int64_t sigma, int32_t maxlen, const int32_t *__restrict__ rp,
+                               uint64_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t row = m - 1 - p;
+        const int32_t len = rp[row + 1] - rp[row];
+        keys[p] = (uint64_t)(row / sigma) * (uint64_t)(maxlen + 1) + (uint64_t)(maxlen - len);
+        vals[p] = (uint32_t)row;
+    }
+}
+
+__global__ void copy_u32_to_i32(int64_t n, const uint32_t *__restrict__ in, int32_t *__restrict__ out) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (int32_t)in[i];
+}
+
+// chunk width = max row length in the chunk, rounded up to `align`
+__global__ void chunk_widths(int64_t m, int32_t C, int32_t align, int64_t nchunks, const int32_t *__restrict__ rp,
+                             const int32_t *__restrict__ reorder, int32_t *__restrict__ width,
+                             int64_t *__restrict__ slots) {
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < nchunks;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        int32_t w = 0;
+        for (int32_t q = 0; q < C; q++) {
+            const int64_t i = c * C + q;
+            if (i >= m) break;
+            const int64_t r = reorder ? reorder[i] : i;
+            w = max(w, rp[r + 1] - rp[r]);
+        }
+        w = ((w + align - 1) / align) * align;
+        width[c] = w;
+        slots[c] = (int64_t)w * C;
+    }
+}
+
+template <typename V>
+__global__ void sliced_fill(int64_t m, int32_t C, const int64_t *__restrict__ chunk_ptr,
+                            const int32_t *__restrict__ reorder, const int32_t *__restrict__ rp,
+                            const int32_t *__restrict__ ci, const V *__restrict__ cv, int32_t *__restrict__ col,
+                            V *__restrict__ val) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = i / C;
+        const int64_t q = i - c * C;
+        const int64_t r = reorder ? reorder[i] : i;
+        const int64_t s0 = rp[r], len = rp[r + 1] - s0;
+        const int64_t base = chunk_ptr[c] + q;
+        for (int64_t k = 0; k < len; k++) {
+            col[base + k * C] = ci[s0 + k];
+            val[base + k * C] = cv[s0 + k];
+        }
+    }
+}
+
+struct SlicedBuild {
+    int32_t *reorder = nullptr;
+    int32_t *width = nullptr;
+    int64_t *chunk_ptr = nullptr;
+    int64_t total = 0;
+    int32_t *col = nullptr;
+    void *val = nullptr;
+    int64_t nchunks = 0;
+    void release(sspmv_stream_t s) {
+        dfree(reorder, s);
+        dfree(width, s);
+        dfree(chunk_ptr, s);
+        dfree(col, s);
+        dfree(val, s);
+        *this = SlicedBuild();
+    }
+};
+
+// sigma: 0 = no reordering (S-ELL / ELL), otherwise the slice height
+// (>= num_rows for SELL-c-R).
+sspmv_status build_sliced(const sspmv_csr *A, int32_t C, int32_t align, int64_t sigma, SlicedBuild &b,
+                          sspmv_stream_t s) {
+    const int64_t m = A->f.num_rows;
+    const int32_t vt = A->f.value_type;
+    b.nchunks = (m + C - 1) / C;
+    int32_t maxlen = 0;
+    SSPMV_TRY(max_row_length(A->row_offset, m, &maxlen, s));
+    const unsigned g = grid_for(m, 256, (int64_t)num_sms() * 16);
+    sspmv_status st = SSPMV_OK;
+    if (sigma > 0) {
+        uint64_t *keys = nullptr;
+        uint32_t *vals = nullptr;
+        st = dalloc(&b.reorder, (size_t)m, s);
+        if (st == SSPMV_OK) st = dalloc(&keys, (size_t)m, s);
+        if (st == SSPMV_OK) st = dalloc(&vals, (size_t)m, s);
+        if (st == SSPMV_OK && m > 0) {
+            sell_sort_keys<<<g, 256, 0, cu(s)>>>(m, sigma, maxlen, A->row_offset, keys, vals);
+            note_launch();
+            const uint64_t nslices = (uint64_t)((m + sigma - 1) / sigma);
+            const uint64_t maxkey = (nslices - 1) * (uint64_t)(maxlen + 1) + (uint64_t)maxlen;
+            st = radix_sort_pairs(keys, vals, m, bits_for(maxkey), s);
+            if (st == SSPMV_OK) {
+                copy_u32_to_i32<<<g, 256, 0, cu(s)>>>(m, vals, b.reorder);
+                note_launch();
+            }
+        }
+        dfree(keys, s);
+        dfree(vals, s);
+        if (st != SSPMV_OK) { b.release(s); return st; }
+    }
+    st = dalloc(&b.width, (size_t)b.nchunks, s);
+    if (st == SSPMV_OK) st = dalloc(&b.chunk_ptr, (size_t)b.nchunks + 1, s);
+    if (st == SSPMV_OK && b.nchunks > 0) {
+        chunk_widths<<<grid_for(b.nchunks, 256, (int64_t)num_sms() * 16), 256, 0, cu(s)>>>(
+            m, C, align, b.nchunks, A->row_offset, b.reorder, b.width, b.chunk_ptr);
+        note_launch();
+        st = exclusive_scan_i64(b.chunk_ptr, b.chunk_ptr, b.nchunks, &b.total, s);
+    }
+    if (st == SSPMV_OK) {
+        cudaError_t e = cudaMemcpyAsync(b.chunk_ptr + b.nchunks, &b.total, 8, cudaMemcpyHostToDevice, cu(s));
+        if (e != cudaSuccess) st = fail(SSPMV_CUDA_ERROR, "chunk_ptr: %s", cudaGetErrorString(e));
+    }
+    if (st == SSPMV_OK) st = dalloc(&b.col, (size_t)b.total, s);
+    if (st == SSPMV_OK) st = dalloc((unsigned char **)&b.val, (size_t)b.total * vsize(vt), s);
+    if (st == SSPMV_OK && b.total > 0) {
+        cudaError_t e = cudaMemsetAsync(b.col, 0xff, (size_t)b.total * 4, cu(s));
+        if (e == cudaSuccess) e = cudaMemsetAsync(b.val, 0, (size_t)b.total * vsize(vt), cu(s));
+        if (e != cudaSuccess) st = fail(SSPMV_CUDA_ERROR, "memset: %s", cudaGetErrorString(e));
+    }
+    if (st == SSPMV_OK && m > 0) {
+        st = dispatch_value(vt, [&](auto tag) -> sspmv_status {
+            using V = decltype(tag);
+            sliced_fill<V><<<g, 256, 0, cu(s)>>>(m, C, b.chunk_ptr, b.reorder, A->row_offset, A->col_index,
+                                                 (const V *)A->values, b.col, (V *)b.val);
+            SSPMV_LAUNCH_CHECK();
+            return SSPMV_OK;
+        });
+    }
+    if (st == SSPMV_OK) {
+        cudaError_t e = cudaStreamSynchronize(cu(s));
+        if (e != cudaSuccess) st = fail(SSPMV_CUDA_ERROR, "convert: %s", cudaGetErrorString(e));
+    }
+    if (st != SSPMV_OK) b.release(s);
+    return st;
+}
+
+sspmv_status check_csr(const sspmv_csr *A) {
+    if (!A) return fail(SSPMV_INVALID_ARG, "null csr");
+    return check_dims(A->f.value_type, A->f.num_rows, A->f.num_cols, A->f.num_nnzs);
+}
+
+// Host copy of a slot-major slab, reordered to the reference's row-major chunks.
+sspmv_status export_slab(const int64_t *d_chunk_ptr, int64_t nchunks, int32_t C, int64_t total, const int32_t *d_col,
+                         const void *d_val, size_t sv, int32_t *col_out, void *val_out, sspmv_stream_t s) {
+    std::vector<int64_t> cp((size_t)nchunks + 1);
+    std::vector<int32_t> col((size_t)std::max<int64_t>(total, 1));
+    std::vector<unsigned char> val((size_t)std::max<int64_t>(total, 1) * sv);
+    SSPMV_CUDA_TRY(cudaMemcpyAsync(cp.data(), d_chunk_ptr, (size_t)(nchunks + 1) * 8, cudaMemcpyDeviceToHost, cu(s)));
+    if (total > 0) {
+        SSPMV_CUDA_TRY(cudaMemcpyAsync(col.data(), d_col, (size_t)total * 4, cudaMemcpyDeviceToHost, cu(s)));
+        SSPMV_CUDA_TRY(cudaMemcpyAsync(val.data(), d_val, (size_t)total * sv, cudaMemcpyDeviceToHost, cu(s)));
+    }
+    SSPMV_CUDA_TRY(cudaStreamSynchronize(cu(s)));
+    for (int64_t c = 0; c < nchunks; c++) {
+        const int64_t base = cp[(size_t)c], w = (cp[(size_t)c + 1] - base) / C;
+        for (int32_t r = 0; r < C; r++)
+            for (int64_t k = 0; k < w; k++) {
+                const int64_t src = base + k * C + r, dst = base + (int64_t)r * w + k;
+                if (col_out) col_out[dst] = col[(size_t)src];
+                if (val_out) std::memcpy((unsigned char *)val_out + dst * sv, val.data() + src * sv, sv);
+            }
+    }
+    return SSPMV_OK;
+}
+
+sspmv_status d2h(void *dst, const void *src, size_t bytes, sspmv_stream_t s) {
+    if (!dst || bytes == 0) return SSPMV_OK;
+    SSPMV_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, cu(s)));
+    SSPMV_CUDA_TRY(cudaStreamSynchronize(cu(s)));
+    return SSPMV_OK;
+}
+
+double sliced_bytes(const sspmv_features *f, int64_t nchunks, bool reorder, int32_t k, int32_t beta_nonzero) {
+    const double sv = (double)vsize(f->value_type);
+    return (double)f->num_nnzs * (sv + 4.0) + (double)(nchunks + 1) * 8.0 +
+           (reorder ? (double)f->num_rows * 4.0 : 0.0) + (double)k * (double)f->num_cols * sv +
+           (double)k * (double)f->num_rows * sv * (beta_nonzero ? 2.0 : 1.0);
+}
+
+}  // namespace
+
+// =================================================================== ELL ===
+extern "C" sspmv_status sspmv_csr_to_ell(const sspmv_csr *csr, int32_t ld, sspmv_ell *out, sspmv_stream_t s) {
+    SSPMV_TRY(check_csr(csr));
+    if (!out) return fail(SSPMV_INVALID_ARG, "null output");
+    if (ld != SSPMV_ROW_MAJOR && ld != SSPMV_COL_MAJOR) return fail(SSPMV_INVALID_ARG, "ld must be 0 or 1");
+    const int64_t m = csr->f.num_rows;
+    int32_t width = 0;
+    SSPMV_TRY(max_row_length(csr->row_offset, m, &width, s));
+    if ((double)m * (double)width > 4.0e9)
+        return fail(SSPMV_INFEASIBLE, "ELL needs %lld x %d slots", (long long)m, width);
+    // ELL == one chunk of C = m rows, alignment 1.
+    SlicedBuild b;
+    SSPMV_TRY(build_sliced(csr, (int32_t)std::max<int64_t>(m, 1), 1, 0, b, s));
+    sspmv_ell A;
+    init_features(&A.f, csr->f.value_type, m, csr->f.num_cols, csr->f.num_nnzs, 1);
+    A.ld = ld;
+    A.max_row_width = width;
+    A.min_row_width = 0;
+    A.col_index = b.col;
+    A.values = b.val;
+    Plan *p = get_plan(&A.f);
+    p->extra[0] = b.chunk_ptr;  // {0, m*width}
+    dfree(b.width, s);
+    *out = A;
+    return SSPMV_OK;
+}
+
+extern "C" sspmv_status sspmv_spmm_ell(double alpha, const sspmv_ell *A, int32_t k, const void *X, int64_t ldx,
+                                       double beta, void *Y, int64_t ldy, sspmv_stream_t s) {
+    if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
+    Plan *p = get_plan(&A->f);
+    SlicedView v{A->f.num_rows, (int32_t)std::max<int64_t>(A->f.num_rows, 1), (const int64_t *)p->extra[0], nullptr,
+                 A->col_index, A->values};
+    return spmm_sliced(&A->f, v, alpha, k, X, ldx, beta, Y, ldy, s);
+}
+
+extern "C" sspmv_status sspmv_LeSpMV_ell(double alpha, const sspmv_ell *A, const void *x, double beta, void *y,
+                                         sspmv_stream_t s) {
+    return sspmv_spmm_ell(alpha, A, 1, x, 1, beta, y, 1, s);
+}
+
+extern "C" sspmv_status sspmv_ell_export(const sspmv_ell *A, int32_t *col_index, void *values, sspmv_stream_t s) {
+    if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
+    const int64_t m = A->f.num_rows, w = A->max_row_width, tot = m * w;
+    const size_t sv = vsize(A->f.value_type);
+    if (A->ld == SSPMV_COL_MAJOR) {
+        SSPMV_TRY(d2h(col_index, A->col_index, (size_t)tot * 4, s));
+        SSPMV_TRY(d2h(values, A->values, (size_t)tot * sv, s));
+        return SSPMV_OK;
+    }
+    std::vector<int32_t> col((size_t)std::max<int64_t>(tot, 1));
+    std::vector<unsigned char> val((size_t)std::max<int64_t>(tot, 1) * sv);
+    SSPMV_TRY(d2h(col.data(), A->col_index, (size_t)tot * 4, s));
+    SSPMV_TRY(d2h(val.data(), A->values, (size_t)tot * sv, s));
+    for (int64_t i = 0; i < m; i++)
+        for (int64_t k = 0; k < w; k++) {
+            if (col_index) col_index[i * w + k] = col[(size_t)(k * m + i)];
+            if (values) std::memcpy((unsigned char *)values + (i * w + k) * sv, val.data() + (k * m + i) * sv, sv);
+        }
+    return SSPMV_OK;
+}
+
+extern "C" sspmv_status sspmv_delete_ell(sspmv_ell *A) {
+    if (!A) return SSPMV_OK;
+    cudaDeviceSynchronize();
+    free_plan(&A->f, nullptr);
+    if (A->f.owns) {
+        dfree(A->col_index, nullptr);
+        dfree(A->values, nullptr);
+    }
+    A->col_index = nullptr;
+    A->values = nullptr;
+    return SSPMV_OK;
+}
+
+extern "C" double sspmv_algorithmic_bytes_ell(const sspmv_ell *A, int32_t k, int32_t beta_nonzero) {
+    return sliced_bytes(&A->f, 0, false, k, beta_nonzero) - 8.0;
+}
+
+// ================================================================= S-ELL ===
+extern "C" sspmv_status sspmv_csr_to_sell(const sspmv_csr *csr, int32_t C, int32_t align, sspmv_s_ell *out,
+                                          sspmv_stream_t s) {
+    SSPMV_TRY(check_csr(csr));
+    if (!out) return fail(SSPMV_INVALID_ARG, "null output");
+    if (C == 0) C = 4;
+    if (align == 0) align = default_alignment(csr->f.value_type);
+    if (C < 1 || align < 1) return fail(SSPMV_INVALID_ARG, "chunkwidth and alignment must be >= 1");
+    SlicedBuild b;
+    SSPMV_TRY(build_sliced(csr, C, align, 0, b, s));
+    sspmv_s_ell A;
+    init_features(&A.f, csr->f.value_type, csr->f.num_rows, csr->f.num_cols, csr->f.num_nnzs, 1);
+    A.sliceWidth = C;
+    A.chunk_num = (int32_t)b.nchunks;
+    A.alignment = align;
+    A.row_width = b.width;
+    A.chunk_ptr = b.chunk_ptr;
+    A.total_slots = b.total;
+    A.col_index = b.col;
+    A.values = b.val;
+    *out = A;
+    return SSPMV_OK;
+}
+
+extern "C" sspmv_status sspmv_spmm_sell(double alpha, const sspmv_s_ell *A, int32_t k, const void *X, int64_t ldx,
+                                        double beta, void *Y, int64_t ldy, sspmv_stream_t s) {
+    if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
+    SlicedView v{A->f.num_rows, A->sliceWidth, A->chunk_ptr, nullptr, A->col_index, A->values};
+    return spmm_sliced(&A->f, v, alpha, k, X, ldx, beta, Y, ldy, s);
+}
+
+extern "C" sspmv_status sspmv_LeSpMV_sell(double alpha, const sspmv_s_ell *A, const void *x, double beta, void *y,
+                                          sspmv_stream_t s) {
+    return sspmv_spmm_sell(alpha, A, 1, x, 1, beta, y, 1, s);
+}
+
+extern "C" sspmv_status sspmv_sell_export(const sspmv_s_ell *A, int32_t *row_width, int32_t *col_index,
+                                          void *values, sspmv_stream_t s) {
+    if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
+    SSPMV_TRY(d2h(row_width, A->row_width, (size_t)A->chunk_num * 4, s));
+    return export_slab(A->chunk_ptr, A->chunk_num, A->sliceWidth, A->total_slots, A->col_index, A->values,
+                       vsize(A->f.value_type), col_index, values, s);
+}
+
+extern "C" sspmv_status sspmv_delete_sell(sspmv_s_ell *A) {
+    if (!A) return SSPMV_OK;
+    cudaDeviceSynchronize();
+    free_plan(&A->f, nullptr);
+    if (A->f.owns) {
+        dfree(A->row_width, nullptr);
+        dfree(A->chunk_ptr, nullptr);
+        dfree(A->col_index, nullptr);
+        dfree(A->values, nullptr);
+    }
+    A->row_width = nullptr;
+    A->chunk_ptr = nullptr;
+    A->col_index = nullptr;
+    A->values = nullptr;
+    return SSPMV_OK;
+}
+
+extern "C" double sspmv_algorithmic_bytes_sell(const sspmv_s_ell *A, int32_t k, int32_t beta_nonzero) {
+    return sliced_bytes(&A->f, A->chunk_num, false, k, beta_nonzero);
+}
+
+// ========================================================== SELL-c-sigma ===
+extern "C" sspmv_status sspmv_csr_to_sell_c_sigma(const sspmv_csr *csr, int32_t sigma, int32_t C, int32_t align,
+                                                  sspmv_sell_c_sigma *out, sspmv_stream_t s) {
+    SSPMV_TRY(check_csr(csr));
+    if (!out) return fail(SSPMV_INVALID_ARG, "null output");
+    if (sigma == 0) sigma = 16384;
+    if (C == 0) C = 4;
+    if (align == 0) align = default_alignment(csr->f.value_type);
+    if (C < 1 || align < 1 || sigma < 1) return fail(SSPMV_INVALID_ARG, "sigma, C and alignment must be >= 1");
+    if (sigma % C) return fail(SSPMV_INVALID_ARG, "sigma (%d) must be a multiple of C (%d)", sigma, C);
+    SlicedBuild b;
+    SSPMV_TRY(build_sliced(csr, C, align, sigma, b, s));
+    const int64_t m = csr->f.num_rows;
+    sspmv_sell_c_sigma A;
+    init_features(&A.f, csr->f.value_type, m, csr->f.num_cols, csr->f.num_nnzs, 1);
+    A.sliceWidth_Sigma = sigma;
+    A.chunkWidth_C = C;
+    A.sliceNum = (int32_t)((m + sigma - 1) / sigma);
+    A.chunk_num_per_slice = sigma / C;
+    A.chunkNum = A.sliceNum * A.chunk_num_per_slice;
+    A.validchunkNum = (int32_t)b.nchunks;
+    A.alignment = align;
+    A.reorder = b.reorder;
+    A.chunk_len = b.width;
+    A.chunk_ptr = b.chunk_ptr;
+    A.total_slots = b.total;
+    A.col_index = b.col;
+    A.values = b.val;
+    *out = A;
+    return SSPMV_OK;
+}
+
+extern "C" sspmv_status sspmv_spmm_sell_c_sigma(double alpha, const sspmv_sell_c_sigma *A, int32_t k, const void *X,
+                                                int64_t ldx, double beta, void *Y, int64_t ldy, sspmv_stream_t s) {
+    if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
+    SlicedView v{A->f.num_rows, A->chunkWidth_C, A->chunk_ptr, A->reorder, A->col_index, A->values};
+    return spmm_sliced(&A->f, v, alpha, k, X, ldx, beta, Y, ldy, s);
+}
+
+extern "C" sspmv_status sspmv_LeSpMV_sell_c_sigma(double alpha, const sspmv_sell_c_sigma *A, const void *x,
+                                                  double beta, void *y, sspmv_stream_t s) {
+    return sspmv_spmm_sell_c_sigma(alpha, A, 1, x, 1, beta, y, 1, s);
+}
+
+extern "C" sspmv_status sspmv_sell_c_sigma_export(const sspmv_sell_c_sigma *A, int32_t *reorder, int32_t *chunk_len,
+                                                  int32_t *col_index, void *values, sspmv_stream_t s) {
+    if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
+    SSPMV_TRY(d2h(reorder, A->reorder, (size_t)A->f.num_rows * 4, s));
+    SSPMV_TRY(d2h(chunk_len, A->chunk_len, (size_t)A->validchunkNum * 4, s));
+    return export_slab(A->chunk_ptr, A->validchunkNum, A->chunkWidth_C, A->total_slots, A->col_index, A->values,
+                       vsize(A->f.value_type), col_index, values, s);
+}
+
+extern "C" sspmv_status sspmv_delete_sell_c_sigma(sspmv_sell_c_sigma *A) {
+    if (!A) return SSPMV_OK;
+    cudaDeviceSynchronize();
+    free_plan(&A->f, nullptr);
+    if (A->f.owns) {
+        dfree(A->reorder, nullptr);
+        dfree(A->chunk_len, nullptr);
+        dfree(A->chunk_ptr, nullptr);
+        dfree(A->col_index, nullptr);
+        dfree(A->values, nullptr);
+    }
+    A->reorder = A->chunk_len = A->col_index = nullptr;
+    A->chunk_ptr = nullptr;
+    A->values = nullptr;
+    return SSPMV_OK;
+}
+
+extern "C" double sspmv_algorithmic_bytes_sell_c_sigma(const sspmv_sell_c_sigma *A, int32_t k, int32_t beta_nonzero) {
+    return sliced_bytes(&A->f, A->validchunkNum, true, k, beta_nonzero);
+}
+
+// ============================================================== SELL-c-R ===
+extern "C" sspmv_status sspmv_csr_to_sell_c_R(const sspmv_csr *csr, int32_t C, int32_t align, sspmv_sell_c_R *out,
+                                              sspmv_stream_t s) {
+    SSPMV_TRY(check_csr(csr));
+    if (!out) return fail(SSPMV_INVALID_ARG, "null output");
+    if (C == 0) C = 4;
+    if (align == 0) align = default_alignment(csr->f.value_type);
+    if (C < 1 || align < 1) return fail(SSPMV_INVALID_ARG, "C and alignment must be >= 1");
+    const int64_t m = csr->f.num_rows;
+    SlicedBuild b;
+    SSPMV_TRY(build_sliced(csr, C, align, std::max<int64_t>(m, 1), b, s));
+    sspmv_sell_c_R A;
+    init_features(&A.f, csr->f.value_type, m, csr->f.num_cols, csr->f.num_nnzs, 1);
+    A.chunkWidth_C = C;
+    A.validchunkNum = (int32_t)b.nchunks;
+    A.alignment = align;
+    A.reorder = b.reorder;
+    A.chunk_len = b.width;
+    A.chunk_ptr = b.chunk_ptr;
+    A.total_slots = b.total;
+    A.col_index = b.col;
+    A.values = b.val;
+    *out = A;
+    return SSPMV_OK;
+}
+
+extern "C" sspmv_status sspmv_spmm_sell_c_R(double alpha, const sspmv_sell_c_R *A, int32_t k, const void *X,
+                                            int64_t ldx, double beta, void *Y, int64_t ldy, sspmv_stream_t s) {
+    if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
+    SlicedView v{A->f.num_rows, A->chunkWidth_C, A->chunk_ptr, A->reorder, A->col_index, A->values};
+    return spmm_sliced(&A->f, v, alpha, k, X, ldx, beta, Y, ldy, s);
+}
+
+extern "C" sspmv_status sspmv_LeSpMV_sell_c_R(double alpha, const sspmv_sell_c_R *A, const void *x, double beta,
+                                              void *y, sspmv_stream_t s) {
+    return sspmv_spmm_sell_c_R(alpha, A, 1, x, 1, beta, y, 1, s);
+}
+
+extern "C" sspmv_status sspmv_sell_c_R_export(const sspmv_sell_c_R *A, int32_t *reorder, int32_t *chunk_len,
+                                              int32_t *col_index, void *values, sspmv_stream_t s) {
+    if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
+    SSPMV_TRY(d2h(reorder, A->reorder, (size_t)A->f.num_rows * 4, s));
+    SSPMV_TRY(d2h(chunk_len, A->chunk_len, (size_t)A->validchunkNum * 4, s));
+    return export_slab(A->chunk_ptr, A->validchunkNum, A->chunkWidth_C, A->total_slots, A->col_index, A->values,
+                       vsize(A->f.value_type), col_index, values, s);
+}
+
+extern "C" sspmv_status sspmv_delete_sell_c_R(sspmv_sell_c_R *A) {
+    if (!A) return SSPMV_OK;
+    cudaDeviceSynchronize();
+    free_plan(&A->f, nullptr);
+    if (A->f.owns) {
+        dfree(A->reorder, nullptr);
+        dfree(A->chunk_len, nullptr);
+        dfree(A->chunk_ptr, nullptr);
+        dfree(A->col_index, nullptr);
+        dfree(A->values, nullptr);
+    }
+    A->reorder = A->chunk_len = A->col_index = nullptr;
+    A->chunk_ptr = nullptr;
+    A->values = nullptr;
+    return SSPMV_OK;
+}
+
+extern "C" double sspmv_algorithmic_bytes_sell_c_R(const sspmv_sell_c_R *A, int32_t k, int32_t beta_nonzero) {
+    return sliced_bytes(&A->f, A->validchunkNum, true, k, beta_nonzero);
+}

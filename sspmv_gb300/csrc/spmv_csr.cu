@@ -17,6 +17,7 @@
 // chosen from the mean row length, or set by the autotuner).
 #include "common.cuh"
 #include "plan.cuh"
+#include "spmv_common.cuh"
 
 namespace sspmv {
 namespace {
@@ -77,14 +78,39 @@ __global__ void __launch_bounds__(kBlock) csr_merge_kernel(
     const int nrows = c1.x - i0, nnzs = c1.y - j0;
 
     // ---- stage row ends and products (coalesced, streaming) ----
-    for (int k = tid; k < nrows; k += kBlock) s_rowend[k] = ld_stream(row_offset + i0 + 1 + k);
-    if (tid == 0) s_row0_start = i0 < m ? row_offset[i0] : 0;
-    for (int k = tid; k < nnzs; k += kBlock) {
-        const int c = ld_stream(col_index + j0 + k);
-        const V a = ld_stream(values + j0 + k);
-        const V *xp = x + (int64_t)c * ldx;
+    // nrows + nnzs <= kTile = kBlock * kItems, so every thread owns at most
+    // kItems nonzeros and kItems row ends; all of its loads are issued before
+    // any is consumed (kItems independent chains in flight per thread).
+    {
+        int cidx[kItems];
+        V aval[kItems];
 #pragma unroll
-        for (int r = 0; r < K; r++) s_prod[k * K + r] = a * ld_x(xp + r);
+        for (int u = 0; u < kItems; u++) {
+            const int k = tid + u * kBlock;
+            cidx[u] = 0;
+            aval[u] = V(0);
+            if (k < nnzs) {
+                cidx[u] = ld_stream(col_index + j0 + k);
+                aval[u] = ld_stream(values + j0 + k);
+            }
+        }
+        int rend[kItems];
+#pragma unroll
+        for (int u = 0; u < kItems; u++) {
+            const int k = tid + u * kBlock;
+            rend[u] = k < nrows ? ld_stream(row_offset + i0 + 1 + k) : 0;
+        }
+        if (tid == 0) s_row0_start = i0 < m ? row_offset[i0] : 0;
+#pragma unroll
+        for (int u = 0; u < kItems; u++) {
+            const int k = tid + u * kBlock;
+            if (k < nnzs) {
+                const V *xp = x + (int64_t)cidx[u] * ldx;
+#pragma unroll
+                for (int r = 0; r < K; r++) s_prod[k * K + r] = aval[u] * ld_x(xp + r);
+            }
+            if (k < nrows) s_rowend[k] = rend[u];
+        }
     }
     __syncthreads();
 
@@ -233,7 +259,21 @@ __global__ void __launch_bounds__(kBlock) csr_vector_kernel(
         for (int r = 0; r < K; r++) s[r] = V(0);
         if (row < m) {
             const int rs = ld_stream(row_offset + row), re = ld_stream(row_offset + row + 1);
-            for (int j = rs + sub; j < re; j += VS) {
+            int j = rs + sub;
+            for (; j + 3 * VS < re; j += 4 * VS) {  // four independent gathers in flight
+                int c[4];
+                V a[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    c[u] = ld_stream(col_index + j + u * VS);
+                    a[u] = ld_stream(values + j + u * VS);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int r = 0; r < K; r++) s[r] += a[u] * ld_x(x + (int64_t)c[u] * ldx + r);
+            }
+            for (; j < re; j += VS) {
                 const int c = ld_stream(col_index + j);
                 const V a = ld_stream(values + j);
 #pragma unroll
@@ -291,7 +331,7 @@ sspmv_status launch_vector_vs(const sspmv_csr *A, V alpha, const V *x, int64_t l
 template <typename V, int K>
 sspmv_status launch_vector(const sspmv_csr *A, Plan *p, V alpha, const V *x, int64_t ldx, V beta, V *y,
                            int64_t ldy, sspmv_stream_t s) {
-    int vs = p->vector_lanes;
+    int vs = p->param;
     if (vs == 0) {
         double mean = A->f.num_rows > 0 ? (double)A->f.num_nnzs / (double)A->f.num_rows : 1.0;
         vs = 2;
@@ -315,20 +355,6 @@ sspmv_status csr_pass(const sspmv_csr *A, Plan *p, V alpha, const V *x, int64_t 
 
 }  // namespace
 
-// Splits k right-hand sides into passes of 8, 4, 2 and 1 columns.
-template <typename V, typename Pass>
-sspmv_status for_rhs_chunks(int32_t k, const V *X, int64_t ldx, V *Y, int64_t ldy, Pass &&pass) {
-    int32_t done = 0;
-    while (done < k) {
-        int32_t left = k - done, step = left >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
-        SSPMV_TRY(pass(step, X + done, Y + done));
-        done += step;
-    }
-    (void)ldx;
-    (void)ldy;
-    return SSPMV_OK;
-}
-
 sspmv_status check_spmm_args(const sspmv_features *f, int32_t k, const void *X, int64_t ldx, const void *Y,
                              int64_t ldy) {
     if (k < 1) return fail(SSPMV_INVALID_ARG, "k must be >= 1 (got %d)", k);
@@ -347,7 +373,7 @@ sspmv_status spmm_csr_impl(double alpha, const sspmv_csr *A, int32_t k, const vo
     if (!p) return fail(SSPMV_OUT_OF_MEMORY, "plan allocation failed");
     return dispatch_value(A->f.value_type, [&](auto tag) -> sspmv_status {
         using V = decltype(tag);
-        return for_rhs_chunks<V>(k, (const V *)X, ldx, (V *)Y, ldy, [&](int32_t step, const V *xs, V *ys) {
+        return for_rhs_chunks<V>(k, (const V *)X, (V *)Y, [&](int32_t step, const V *xs, V *ys) {
             const V a = (V)alpha, b = (V)beta;
             switch (step) {
             case 8: return csr_pass<V, 8>(A, p, a, xs, ldx, b, ys, ldy, s);

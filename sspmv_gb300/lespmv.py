@@ -80,6 +80,10 @@ class Matrix:
     def ref(self):
         return C.byref(self.s)
 
+    def set_kernel(self, kernel_flag: int, param: int = 0) -> None:
+        """Selects the SpMV kernel (sspmv_set_kernel)."""
+        call("sspmv_set_kernel", C.byref(self.s.f), int(kernel_flag), int(param))
+
     def delete(self) -> None:
         if self._alive:
             self._alive = False
@@ -105,6 +109,83 @@ class CSR_Matrix(Matrix):
         call("sspmv_csr_export", self.ref(), rp.ctypes.data_as(C.c_void_p), col.ctypes.data_as(C.c_void_p),
              val.ctypes.data_as(C.c_void_p), _stream(stream))
         return {"row_offset": rp, "col": col, "val": val}
+
+
+def _host(n, dtype):
+    a = np.empty(max(int(n), 0), dtype)
+    return a, a.ctypes.data_as(C.c_void_p)
+
+
+class ELL_Matrix(Matrix):
+    fmt = "ell"
+
+    def export(self, stream=None) -> dict:
+        n = self.num_rows * self.s.max_row_width
+        col, pc = _host(n, np.int32)
+        val, pv = _host(n, self.dtype)
+        call("sspmv_ell_export", self.ref(), pc, pv, _stream(stream))
+        return {"max_row_width": int(self.s.max_row_width), "col": col, "val": val}
+
+
+class SELL_Matrix(Matrix):
+    """S_ELL_Matrix (sliced ELLPACK)."""
+    fmt = "sell"
+
+    def export(self, stream=None) -> dict:
+        rw, pr = _host(self.s.chunk_num, np.int32)
+        col, pc = _host(self.s.total_slots, np.int32)
+        val, pv = _host(self.s.total_slots, self.dtype)
+        call("sspmv_sell_export", self.ref(), pr, pc, pv, _stream(stream))
+        return {"chunk_num": int(self.s.chunk_num), "row_width": rw, "col": col, "val": val}
+
+
+class _SellReordered(Matrix):
+    def export(self, stream=None) -> dict:
+        ro, pro = _host(self.num_rows, np.int32)
+        cl, pcl = _host(self.s.validchunkNum, np.int32)
+        col, pc = _host(self.s.total_slots, np.int32)
+        val, pv = _host(self.s.total_slots, self.dtype)
+        call(f"sspmv_{self.fmt}_export", self.ref(), pro, pcl, pc, pv, _stream(stream))
+        return {"reorder": ro, "chunk_len": cl, "col": col, "val": val,
+                "validchunkNum": int(self.s.validchunkNum)}
+
+
+class SELL_C_Sigma_Matrix(_SellReordered):
+    fmt = "sell_c_sigma"
+
+
+class SELL_C_R_Matrix(_SellReordered):
+    fmt = "sell_c_R"
+
+
+def csr_to_ell(csr: CSR_Matrix, ld: int = RowMajor, stream=None) -> ELL_Matrix:
+    """csr_to_ell (include/sparse_conversion.h:187-248)."""
+    s = _lib.Ell()
+    call("sspmv_csr_to_ell", csr.ref(), int(ld), C.byref(s), _stream(stream))
+    return ELL_Matrix(s)
+
+
+def csr_to_sell(csr: CSR_Matrix, chunkwidth: int = 0, alignment: int = 0, stream=None) -> SELL_Matrix:
+    """csr_to_sell (include/sparse_conversion.h:258-334); 0 = reference default."""
+    s = _lib.SEll()
+    call("sspmv_csr_to_sell", csr.ref(), int(chunkwidth), int(alignment), C.byref(s), _stream(stream))
+    return SELL_Matrix(s)
+
+
+def csr_to_sell_c_sigma(csr: CSR_Matrix, slicewidth: int = 0, chunkwidth: int = 0, alignment: int = 0,
+                        stream=None) -> SELL_C_Sigma_Matrix:
+    """csr_to_sell_c_sigma (include/sparse_conversion.h:337-479)."""
+    s = _lib.SellCSigma()
+    call("sspmv_csr_to_sell_c_sigma", csr.ref(), int(slicewidth), int(chunkwidth), int(alignment), C.byref(s),
+         _stream(stream))
+    return SELL_C_Sigma_Matrix(s)
+
+
+def csr_to_sell_c_R(csr: CSR_Matrix, chunkwidth: int = 0, alignment: int = 0, stream=None) -> SELL_C_R_Matrix:
+    """csr_to_sell_c_R (include/sparse_conversion.h:483-598)."""
+    s = _lib.SellCR()
+    call("sspmv_csr_to_sell_c_R", csr.ref(), int(chunkwidth), int(alignment), C.byref(s), _stream(stream))
+    return SELL_C_R_Matrix(s)
 
 
 def csr_from_host(A: HostCSR, stream=None) -> CSR_Matrix:
@@ -157,9 +238,9 @@ def LeSpMV_csr(alpha, A: CSR_Matrix, x, beta, y, stream=None) -> None:
 
 
 # Formats the library builds, in benchmark order.
-FORMATS = ["csr"]
+FORMATS = ["csr", "ell", "sell", "sell_c_sigma", "sell_c_R"]
 # Formats the smoke check converts from CSR (besides CSR itself).
-SMOKE_FORMATS: list[str] = []
+SMOKE_FORMATS: list[str] = ["ell", "sell", "sell_c_sigma", "sell_c_R"]
 
 
 def bsr_block_for(A: HostCSR) -> tuple[int, int]:

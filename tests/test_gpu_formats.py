@@ -1,0 +1,153 @@
+"""GPU converters and kernels of every format except CSR, through the C ABI.
+
+Converters: the exported arrays (reference layout) must be bit-identical to
+the reference's own converter output (golden fixture digests) and to the
+oracle restatement on larger seeded matrices.
+SpMV / SpMM: per-row bound |y_i - y_ref_i| <= 8*nnz_i*eps*|alpha|*sum_j|a_ij
+x_j| + 2*eps*|beta*y0_i| against the FP64 CSR result (y_ref) on the same
+inputs, FP64 and FP32."""
+import numpy as np
+import pytest
+
+from golden_util import ALPHA, BETA, digest, files, load
+from gpu_util import to_dev, to_host
+from oracle import tolerance_ok
+
+pytestmark = pytest.mark.gpu
+
+CASES = files()
+
+
+def gpu_convert(L, M, fn, kw):
+    """Runs the library converter named like the oracle's, mapping its kwargs."""
+    if fn == "csr_to_ell":
+        return L.csr_to_ell(M, kw.get("ld", 0))
+    if fn == "csr_to_sell":
+        return L.csr_to_sell(M, kw.get("C_", 0), kw.get("align", 0) or 0)
+    if fn == "csr_to_sell_c_sigma":
+        return L.csr_to_sell_c_sigma(M, kw.get("sigma", 0), kw.get("C_", 0), kw.get("align", 0) or 0)
+    if fn == "csr_to_sell_c_R":
+        return L.csr_to_sell_c_R(M, kw.get("C_", 0), kw.get("align", 0) or 0)
+    if fn == "csr_to_dia" and hasattr(L, "csr_to_dia"):
+        return L.csr_to_dia(M, kw.get("max_diags", 0), kw.get("align", 0) or 0)
+    if fn == "csr_to_bsr" and hasattr(L, "csr_to_bsr"):
+        return L.csr_to_bsr(M, kw.get("r", 0), kw.get("c", 0) or 0)
+    if fn == "csr_to_csr5" and hasattr(L, "csr_to_csr5"):
+        return L.csr_to_csr5(M)
+    return None
+
+
+@pytest.mark.parametrize("path", CASES, ids=[p.stem for p in CASES])
+def test_converters_match_reference(path):
+    from sspmv_gb300 import lespmv as L
+    z, meta, A = load(path)
+    M = L.csr_from_host(A)
+    checked = 0
+    for key, rec in meta["conv"].items():
+        G = gpu_convert(L, M, rec["fn"], rec["kw"])
+        if G is None:
+            continue
+        out = G.export()
+        for name, d in rec["digests"].items():
+            assert name in out, (key, name)
+            assert list(out[name].shape) == rec["shapes"][name], (key, name, out[name].shape)
+            assert digest(out[name]) == d, f"{path.stem}:{key}:{name} differs from the reference"
+        for name, v in rec["scalars"].items():
+            if name in out:
+                assert int(out[name]) == v, (key, name)
+        checked += 1
+    assert checked >= 9
+
+
+SPMV_FORMATS = [("ell", "csr_to_ell", {}), ("sell", "csr_to_sell", {}), ("sell_c_sigma", "csr_to_sell_c_sigma", {}),
+                ("sell_c_R", "csr_to_sell_c_R", {}), ("dia", "csr_to_dia", {}), ("bsr", "csr_to_bsr", {}),
+                ("coo", "csr_to_coo", {}), ("csr5", "csr_to_csr5", {})]
+
+
+@pytest.mark.parametrize("path", CASES, ids=[p.stem for p in CASES])
+def test_spmv_golden(path, oracle_lib):
+    from sspmv_gb300 import lespmv as L
+    z, meta, A = load(path)
+    dt = A.values.dtype
+    x, y0 = z["x"], z["y0"]
+    y64, absum = oracle_lib.spmm_ref(A, x, ALPHA, BETA, y0)
+    nnz_row = np.diff(A.row_offset)
+    has_dups = "in_coo_row" in z.files
+    M = L.csr_from_host(A)
+    for fmt, fn, kw in SPMV_FORMATS:
+        conv = getattr(L, fn, None)
+        if conv is None:
+            continue
+        try:
+            G = conv(M, **kw)
+        except L.SSPMVError as e:
+            assert e.status == 2 and fmt == "dia", (fmt, e)  # DIA over max_diags
+            continue
+        y = to_dev(y0)
+        L.LeSpMV(ALPHA, G, to_dev(x), BETA, y)
+        yg = to_host(y)
+        if has_dups and fmt in ("dia", "bsr"):
+            yr = z.get(f"y_{fmt}_1")  # duplicates overwrite: compare with the reference itself
+            assert oracle_lib.max_rel_error(yg, yr) < 5 * np.sqrt(np.finfo(dt).eps), fmt
+            continue
+        ok, mx, med = tolerance_ok(yg, y64, absum, nnz_row, dt, ALPHA, BETA, y0)
+        assert ok, f"{fmt}: max normalised error {mx}"
+
+
+FAMILIES = {
+    "powerlaw": lambda s: s.powerlaw(30000, 1.8, 16.0, 3000, 0.02),
+    "uniform": lambda s: s.uniform(20000, 32, 0.01),
+    "banded": lambda s: s.banded(30000),
+    "block": lambda s: s.block(20000, 4, 4000),
+    "wide": lambda s: s.uniform(5000, 12, 0.05, num_cols=17000),
+}
+
+ORACLE_CONV = {
+    "ell": lambda O, A: O.csr_to_ell(A, 0),
+    "sell": lambda O, A: O.csr_to_sell(A, 8, 4),
+    "sell_c_sigma": lambda O, A: O.csr_to_sell_c_sigma(A, 256, 32, 1),
+    "sell_c_R": lambda O, A: O.csr_to_sell_c_R(A, 16),
+}
+GPU_CONV = {
+    "ell": lambda L, M: L.csr_to_ell(M, 0),
+    "sell": lambda L, M: L.csr_to_sell(M, 8, 4),
+    "sell_c_sigma": lambda L, M: L.csr_to_sell_c_sigma(M, 256, 32, 1),
+    "sell_c_R": lambda L, M: L.csr_to_sell_c_R(M, 16),
+}
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
+@pytest.mark.parametrize("fam", list(FAMILIES))
+def test_families_convert_and_spmm(fam, dt, oracle_lib):
+    from sspmv_gb300 import lespmv as L
+    from sspmv_gb300 import synth
+    A = synth.generate(FAMILIES[fam](synth), 3, dt)
+    M = L.csr_from_host(A)
+    nnz_row = np.diff(A.row_offset)
+    for fmt in GPU_CONV:
+        if fmt == "ell" and fam == "powerlaw":
+            continue
+        G = GPU_CONV[fmt](L, M)
+        ref = ORACLE_CONV[fmt](oracle_lib, A)
+        out = G.export()
+        for name, arr in ref.items():
+            if isinstance(arr, np.ndarray):
+                assert np.array_equal(out[name].view(np.uint8), arr.view(np.uint8)), (fam, fmt, name)
+        for k in (1, 3, 8):
+            X = synth.vector(A.num_cols, 0, dt, k).reshape(A.num_cols, k)
+            Y0 = synth.vector(A.num_rows, 9, dt, k).reshape(A.num_rows, k)
+            Y = to_dev(Y0)
+            L.spmm(ALPHA, G, to_dev(X), BETA, Y)
+            y64, absum = oracle_lib.spmm_ref(A, X, ALPHA, BETA, Y0)
+            ok, mx, _ = tolerance_ok(to_host(Y), y64, absum, nnz_row, dt, ALPHA, BETA, Y0)
+            assert ok, f"{fam}/{fmt}/k={k}: max normalised error {mx}"
+
+
+def test_sigma_not_multiple_of_c_is_rejected():
+    from sspmv_gb300 import lespmv as L
+    from sspmv_gb300 import synth
+    A = synth.generate(synth.uniform(1000, 8), 1)
+    M = L.csr_from_host(A)
+    with pytest.raises(L.SSPMVError) as e:
+        L.csr_to_sell_c_sigma(M, 100, 8)
+    assert e.value.status == 1
