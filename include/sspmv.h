@@ -156,6 +156,31 @@ typedef struct {
     void *values;
 } sspmv_sell_c_R;
 
+/* DIA_Matrix (include/sparse_format.h:173-185): diagonal d (offset
+ * diag_offsets[d]) stored at diag_data[d*stride + row], zero filled. */
+typedef struct {
+    sspmv_features f;
+    int32_t stride;
+    int32_t complete_ndiags;
+    int64_t *diag_offsets;
+    void *diag_data;
+} sspmv_dia;
+
+/* BSR_Matrix (include/sparse_format.h:113-130): blockDim_r x blockDim_c
+ * blocks, row-major inside a block, block columns ascending per block row. */
+typedef struct {
+    sspmv_features f;
+    int64_t blockDim_r;
+    int64_t blockDim_c;
+    int64_t blockNNZ;
+    int64_t mb;
+    int64_t nb;
+    int64_t nnzb;
+    int32_t *row_ptr;        /* [mb + 1] */
+    int32_t *block_colindex; /* [nnzb] */
+    void *block_data;        /* [nnzb * blockNNZ] */
+} sspmv_bsr;
+
 /* ---------------- status / memory ---------------- */
 const char *sspmv_status_string(sspmv_status s);
 const char *sspmv_last_error(void);
@@ -248,9 +273,61 @@ sspmv_status sspmv_sell_c_R_export(const sspmv_sell_c_R *A, int32_t *reorder, in
                                    int32_t *col_index, void *values, sspmv_stream_t stream);
 sspmv_status sspmv_delete_sell_c_R(sspmv_sell_c_R *A);
 
+/* ---------------- COO ---------------- */
+/* Device COO from arrays (from_host as sspmv_csr_create); row_sorted is set
+ * when the host rows are non-decreasing (device input: 0). */
+sspmv_status sspmv_coo_create(sspmv_coo *out, int32_t value_type, int64_t num_rows, int64_t num_cols,
+                              int64_t num_nnzs, const int32_t *row_index, const int32_t *col_index,
+                              const void *values, int32_t from_host, sspmv_stream_t stream);
+/* csr_to_coo (include/sparse_conversion.h:145-168) */
+sspmv_status sspmv_csr_to_coo(const sspmv_csr *csr, sspmv_coo *out, sspmv_stream_t stream);
+/* coo_to_csr (include/sparse_conversion.h:30-91, compact = false) */
+sspmv_status sspmv_coo_to_csr(const sspmv_coo *coo, sspmv_csr *out, sspmv_stream_t stream);
+/* LeSpMV_coo (src/spmv_coo.cpp:161-182) */
+sspmv_status sspmv_LeSpMV_coo(double alpha, const sspmv_coo *A, const void *x, double beta, void *y,
+                              sspmv_stream_t stream);
+sspmv_status sspmv_spmm_coo(double alpha, const sspmv_coo *A, int32_t k, const void *X, int64_t ldx,
+                            double beta, void *Y, int64_t ldy, sspmv_stream_t stream);
+sspmv_status sspmv_coo_export(const sspmv_coo *A, int32_t *row_index, int32_t *col_index, void *values,
+                              sspmv_stream_t stream);
+sspmv_status sspmv_delete_coo(sspmv_coo *A);
+
+/* ---------------- DIA ---------------- */
+/* csr_to_dia (include/sparse_conversion.h:612-766); max_diags / alignment 0
+ * = defaults (10240, 64/sizeof(value)); more diagonals -> SSPMV_INFEASIBLE. */
+sspmv_status sspmv_csr_to_dia(const sspmv_csr *csr, int32_t max_diags, int32_t alignment, sspmv_dia *out,
+                              sspmv_stream_t stream);
+/* LeSpMV_dia (src/spmv_dia.cpp:177-197) */
+sspmv_status sspmv_LeSpMV_dia(double alpha, const sspmv_dia *A, const void *x, double beta, void *y,
+                              sspmv_stream_t stream);
+sspmv_status sspmv_spmm_dia(double alpha, const sspmv_dia *A, int32_t k, const void *X, int64_t ldx,
+                            double beta, void *Y, int64_t ldy, sspmv_stream_t stream);
+/* diag_offsets: complete_ndiags; diag_data: complete_ndiags*stride */
+sspmv_status sspmv_dia_export(const sspmv_dia *A, int64_t *diag_offsets, void *diag_data, sspmv_stream_t stream);
+sspmv_status sspmv_delete_dia(sspmv_dia *A);
+
+/* ---------------- BSR ---------------- */
+/* csr_to_bsr (include/sparse_conversion.h:769-926); 0 = defaults
+ * (16 x 64/sizeof(value)). */
+sspmv_status sspmv_csr_to_bsr(const sspmv_csr *csr, int32_t blockDimRow, int32_t blockDimCol, sspmv_bsr *out,
+                              sspmv_stream_t stream);
+/* LeSpMV_bsr (src/spmv_bsr.cpp:215-233) */
+sspmv_status sspmv_LeSpMV_bsr(double alpha, const sspmv_bsr *A, const void *x, double beta, void *y,
+                              sspmv_stream_t stream);
+sspmv_status sspmv_spmm_bsr(double alpha, const sspmv_bsr *A, int32_t k, const void *X, int64_t ldx,
+                            double beta, void *Y, int64_t ldy, sspmv_stream_t stream);
+/* row_ptr: mb+1 (num_rows+1 for 1x1 blocks); block_colindex: nnzb;
+ * block_data: nnzb*blockNNZ */
+sspmv_status sspmv_bsr_export(const sspmv_bsr *A, int32_t *row_ptr, int32_t *block_colindex, void *block_data,
+                              sspmv_stream_t stream);
+sspmv_status sspmv_delete_bsr(sspmv_bsr *A);
+
 /* Algorithmic bytes of one SpMV with k right-hand sides: structural bytes of
  * the format (padding excluded) + x once + y once (twice when beta != 0). */
 double sspmv_algorithmic_bytes_csr(const sspmv_csr *A, int32_t k, int32_t beta_nonzero);
+double sspmv_algorithmic_bytes_coo(const sspmv_coo *A, int32_t k, int32_t beta_nonzero);
+double sspmv_algorithmic_bytes_dia(const sspmv_dia *A, int32_t k, int32_t beta_nonzero);
+double sspmv_algorithmic_bytes_bsr(const sspmv_bsr *A, int32_t k, int32_t beta_nonzero);
 double sspmv_algorithmic_bytes_ell(const sspmv_ell *A, int32_t k, int32_t beta_nonzero);
 double sspmv_algorithmic_bytes_sell(const sspmv_s_ell *A, int32_t k, int32_t beta_nonzero);
 double sspmv_algorithmic_bytes_sell_c_sigma(const sspmv_sell_c_sigma *A, int32_t k, int32_t beta_nonzero);

@@ -71,6 +71,17 @@ class SellCR(C.Structure):
                 ("total_slots", C.c_int64), ("col_index", P32), ("values", C.c_void_p)]
 
 
+class Dia(C.Structure):
+    _fields_ = [("f", Features), ("stride", C.c_int32), ("complete_ndiags", C.c_int32), ("diag_offsets", P64),
+                ("diag_data", C.c_void_p)]
+
+
+class Bsr(C.Structure):
+    _fields_ = [("f", Features), ("blockDim_r", C.c_int64), ("blockDim_c", C.c_int64), ("blockNNZ", C.c_int64),
+                ("mb", C.c_int64), ("nb", C.c_int64), ("nnzb", C.c_int64), ("row_ptr", P32),
+                ("block_colindex", P32), ("block_data", C.c_void_p)]
+
+
 class SynthParams(C.Structure):
     _fields_ = [("family", C.c_int32), ("num_offsets", C.c_int32), ("num_rows", C.c_int64),
                 ("num_cols", C.c_int64), ("grid", C.c_int64), ("offsets", C.c_int64 * 32),
@@ -141,6 +152,11 @@ _SIGS.update(_format_sigs("ell", Ell, [_i32], [_vp, _vp]))
 _SIGS.update(_format_sigs("sell", SEll, [_i32, _i32], [_vp, _vp, _vp]))
 _SIGS.update(_format_sigs("sell_c_sigma", SellCSigma, [_i32, _i32, _i32], [_vp, _vp, _vp, _vp]))
 _SIGS.update(_format_sigs("sell_c_R", SellCR, [_i32, _i32], [_vp, _vp, _vp, _vp]))
+_SIGS.update(_format_sigs("coo", Coo, [], [_vp, _vp, _vp]))
+_SIGS.update(_format_sigs("dia", Dia, [_i32, _i32], [_vp, _vp]))
+_SIGS.update(_format_sigs("bsr", Bsr, [_i32, _i32], [_vp, _vp, _vp]))
+_SIGS["sspmv_coo_create"] = (_st, [C.POINTER(Coo), _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp])
+_SIGS["sspmv_coo_to_csr"] = (_st, [C.POINTER(Coo), C.POINTER(Csr), _vp])
 
 for _n, (_r, _a) in _SIGS.items():
     register(_n, _r, _a)

@@ -1,0 +1,313 @@
+// bsr.cu -- BSR format on sm_103a: GPU converter, SpMV / SpMM, export.
+//
+// Converter (csr_to_bsr, include/sparse_conversion.h:769-926): the distinct
+// (block row, block column) pairs of the nonzeros, block columns ascending in
+// each block row, blocks stored row-major (r x c) and zero filled.  On the GPU
+// every nonzero contributes the key block_row*nb + block_col, the keys are
+// radix sorted and made unique, and values are written row by row in CSR
+// order (a duplicated (row, col) keeps its last value, as the reference's
+// overwrite).  r = c = 1 copies the CSR arrays, as the reference does.
+//
+// SpMV (LeSpMV_bsr, src/spmv_bsr.cpp:215-233): one thread per matrix row.  The
+// r threads of a block row read the r consecutive c-wide rows of each block,
+// so a block (r*c values) is one contiguous read; x[bc*c .. bc*c+c) is one
+// c-wide read shared by the r threads.  Columns past num_cols (the ragged
+// last block column) are skipped.
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+#include "plan.cuh"
+#include "primitives.cuh"
+#include "spmv_common.cuh"
+
+namespace sspmv {
+sspmv_status check_dims(int32_t vt, int64_t m, int64_t n, int64_t nnz);
+void init_features(sspmv_features *f, int32_t vt, int64_t m, int64_t n, int64_t nnz, int32_t owns);
+}  // namespace sspmv
+
+using namespace sspmv;
+
+namespace {
+
+constexpr int kBlock = 256;
+
+__global__ void bsr_keys(int64_t m, int32_t r, int32_t c, int64_t nb, const int32_t *__restrict__ rp,
+                         const int32_t *__restrict__ ci, uint64_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t br = (uint64_t)(i / r);
+        for (int32_t jj = rp[i]; jj < rp[i + 1]; jj++) {
+            keys[jj] = br * (uint64_t)nb + (uint64_t)(ci[jj] / c);
+            vals[jj] = (uint32_t)jj;
+        }
+    }
+}
+
+__global__ void unique_flags(int64_t n, const uint64_t *__restrict__ keys, int32_t *__restrict__ flags) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        flags[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
+}
+
+__global__ void unique_scatter(int64_t n, const uint64_t *__restrict__ keys, const int32_t *__restrict__ pos,
+                               int64_t nb, uint64_t *__restrict__ ukeys, int32_t *__restrict__ bcol) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (i == 0 || keys[i] != keys[i - 1]) {
+            ukeys[pos[i]] = keys[i];
+            bcol[pos[i]] = (int32_t)(keys[i] % (uint64_t)nb);
+        }
+}
+
+// row_ptr[b] = first unique block with block row >= b
+__global__ void bsr_row_ptr(int64_t mb, int64_t nb, int64_t nnzb, const uint64_t *__restrict__ ukeys,
+                            int32_t *__restrict__ row_ptr) {
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b <= mb; b += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t key = (uint64_t)b * (uint64_t)nb;
+        int64_t lo = 0, hi = nnzb;
+        while (lo < hi) {
+            int64_t mid = (lo + hi) >> 1;
+            if (ukeys[mid] < key) lo = mid + 1;
+            else hi = mid;
+        }
+        row_ptr[b] = (int32_t)lo;
+    }
+}
+
+template <typename V>
+__global__ void bsr_fill(int64_t m, int32_t r, int32_t c, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
+                         const V *__restrict__ cv, const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ bcol,
+                         V *__restrict__ data) {
+    const int64_t rc = (int64_t)r * c;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t br = i / r, q = i - br * r;
+        const int32_t b0 = row_ptr[br], b1 = row_ptr[br + 1];
+        for (int32_t jj = rp[i]; jj < rp[i + 1]; jj++) {
+            const int32_t col = ci[jj], bc = col / c;
+            int32_t lo = b0, hi = b1;
+            while (lo < hi) {
+                int32_t mid = (lo + hi) >> 1;
+                if (bcol[mid] < bc) lo = mid + 1;
+                else hi = mid;
+            }
+            data[(int64_t)lo * rc + q * c + (col - bc * c)] = cv[jj];
+        }
+    }
+}
+
+template <typename V, int K, int CB>
+__global__ void __launch_bounds__(kBlock) bsr_spmv_kernel(int m, int n, int r, int cr,
+                                                        const int32_t *__restrict__ row_ptr,
+                                                        const int32_t *__restrict__ bcol, const V *__restrict__ data,
+                                                        const V *__restrict__ x, int64_t ldx, V alpha, V beta,
+                                                        V *__restrict__ y, int64_t ldy) {
+    const int c = CB > 0 ? CB : cr;
+    const int64_t rc = (int64_t)r * c;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t br = i / r, q = i - br * r;
+        const int32_t k0 = ld_stream(row_ptr + br), k1 = ld_stream(row_ptr + br + 1);
+        V s[K];
+#pragma unroll
+        for (int t = 0; t < K; t++) s[t] = V(0);
+        for (int32_t k = k0; k < k1; k++) {
+            const int64_t x0 = (int64_t)ld_x(bcol + k) * c;
+            const V *blk = data + k * rc + q * c;
+            if (CB > 0 && x0 + c <= n) {
+                V a[CB > 0 ? CB : 1];
+#pragma unroll
+                for (int e = 0; e < (CB > 0 ? CB : 1); e++) a[e] = ld_stream(blk + e);
+#pragma unroll
+                for (int e = 0; e < (CB > 0 ? CB : 1); e++)
+#pragma unroll
+                    for (int t = 0; t < K; t++) s[t] += a[e] * ld_x(x + (x0 + e) * ldx + t);
+            } else {
+                for (int e = 0; e < c; e++) {
+                    if (x0 + e >= n) break;
+                    const V a = ld_stream(blk + e);
+#pragma unroll
+                    for (int t = 0; t < K; t++) s[t] += a * ld_x(x + (x0 + e) * ldx + t);
+                }
+            }
+        }
+        V *yp = y + i * ldy;
+#pragma unroll
+        for (int t = 0; t < K; t++) yp[t] = axpby(alpha, s[t], beta, yp + t);
+    }
+}
+
+template <typename V, int K, int CB>
+sspmv_status launch_bsr_c(const sspmv_bsr *A, V alpha, const V *x, int64_t ldx, V beta, V *y, int64_t ldy,
+                          sspmv_stream_t s) {
+    const unsigned grid = grid_for(A->f.num_rows, kBlock, (int64_t)num_sms() * 16);
+    bsr_spmv_kernel<V, K, CB><<<grid, kBlock, 0, cu(s)>>>((int)A->f.num_rows, (int)A->f.num_cols, (int)A->blockDim_r,
+                                                          (int)A->blockDim_c, A->row_ptr, A->block_colindex,
+                                                          (const V *)A->block_data, x, ldx, alpha, beta, y, ldy);
+    SSPMV_LAUNCH_CHECK();
+    return SSPMV_OK;
+}
+
+template <typename V, int K>
+sspmv_status launch_bsr(const sspmv_bsr *A, V alpha, const V *x, int64_t ldx, V beta, V *y, int64_t ldy,
+                        sspmv_stream_t s) {
+    switch (A->blockDim_c) {
+    case 1: return launch_bsr_c<V, K, 1>(A, alpha, x, ldx, beta, y, ldy, s);
+    case 2: return launch_bsr_c<V, K, 2>(A, alpha, x, ldx, beta, y, ldy, s);
+    case 4: return launch_bsr_c<V, K, 4>(A, alpha, x, ldx, beta, y, ldy, s);
+    case 8: return launch_bsr_c<V, K, 8>(A, alpha, x, ldx, beta, y, ldy, s);
+    case 16: return launch_bsr_c<V, K, 16>(A, alpha, x, ldx, beta, y, ldy, s);
+    default: return launch_bsr_c<V, K, 0>(A, alpha, x, ldx, beta, y, ldy, s);
+    }
+}
+
+}  // namespace
+
+extern "C" sspmv_status sspmv_csr_to_bsr(const sspmv_csr *csr, int32_t r, int32_t c, sspmv_bsr *out,
+                                         sspmv_stream_t s) {
+    if (!csr || !out) return fail(SSPMV_INVALID_ARG, "null argument");
+    SSPMV_TRY(check_dims(csr->f.value_type, csr->f.num_rows, csr->f.num_cols, csr->f.num_nnzs));
+    if (r == 0) r = 16;
+    if (c == 0) c = default_alignment(csr->f.value_type);
+    if (r < 1 || c < 1) return fail(SSPMV_INVALID_ARG, "block dimensions must be >= 1");
+    const int64_t m = csr->f.num_rows, n = csr->f.num_cols, nnz = csr->f.num_nnzs;
+    const int32_t vt = csr->f.value_type;
+    const size_t sv = vsize(vt);
+    sspmv_bsr A;
+    init_features(&A.f, vt, m, n, nnz, 1);
+    A.blockDim_r = r;
+    A.blockDim_c = c;
+    A.blockNNZ = (int64_t)r * c;
+    A.mb = (m + r - 1) / r;
+    A.nb = (n + c - 1) / c;
+    A.row_ptr = nullptr;
+    A.block_colindex = nullptr;
+    A.block_data = nullptr;
+    const unsigned g = grid_for(std::max<int64_t>(m, 1), 256, (int64_t)num_sms() * 16);
+    sspmv_status st = SSPMV_OK;
+    if (r == 1 && c == 1) {  // include/sparse_conversion.h:784-815: copies of the CSR arrays
+        A.nnzb = nnz;
+        st = dalloc(&A.row_ptr, (size_t)m + 1, s);
+        if (st == SSPMV_OK) st = dalloc(&A.block_colindex, (size_t)nnz, s);
+        if (st == SSPMV_OK) st = dalloc((unsigned char **)&A.block_data, (size_t)nnz * sv, s);
+        if (st == SSPMV_OK) {
+            cudaError_t e = cudaMemcpyAsync(A.row_ptr, csr->row_offset, ((size_t)m + 1) * 4, cudaMemcpyDeviceToDevice, cu(s));
+            if (e == cudaSuccess && nnz)
+                e = cudaMemcpyAsync(A.block_colindex, csr->col_index, (size_t)nnz * 4, cudaMemcpyDeviceToDevice, cu(s));
+            if (e == cudaSuccess && nnz)
+                e = cudaMemcpyAsync(A.block_data, csr->values, (size_t)nnz * sv, cudaMemcpyDeviceToDevice, cu(s));
+            if (e == cudaSuccess) e = cudaStreamSynchronize(cu(s));
+            if (e != cudaSuccess) st = fail(SSPMV_CUDA_ERROR, "csr_to_bsr copy: %s", cudaGetErrorString(e));
+        }
+    } else {
+        uint64_t *keys = nullptr, *ukeys = nullptr;
+        uint32_t *vals = nullptr;
+        int32_t *pos = nullptr;
+        int32_t nnzb = 0;
+        st = dalloc(&keys, (size_t)nnz, s);
+        if (st == SSPMV_OK) st = dalloc(&vals, (size_t)nnz, s);
+        if (st == SSPMV_OK) st = dalloc(&pos, (size_t)nnz, s);
+        if (st == SSPMV_OK && nnz > 0) {
+            bsr_keys<<<g, 256, 0, cu(s)>>>(m, r, c, A.nb, csr->row_offset, csr->col_index, keys, vals);
+            note_launch();
+            st = radix_sort_pairs(keys, vals, nnz, bits_for((uint64_t)(A.mb * A.nb)), s);
+            if (st == SSPMV_OK) {
+                unique_flags<<<grid_for(nnz, 256, (int64_t)num_sms() * 16), 256, 0, cu(s)>>>(nnz, keys, pos);
+                note_launch();
+                st = exclusive_scan_i32(pos, pos, nnz, &nnzb, s);
+            }
+        }
+        A.nnzb = nnzb;
+        if (st == SSPMV_OK) st = dalloc(&ukeys, (size_t)nnzb, s);
+        if (st == SSPMV_OK) st = dalloc(&A.block_colindex, (size_t)nnzb, s);
+        if (st == SSPMV_OK) st = dalloc(&A.row_ptr, (size_t)A.mb + 1, s);
+        if (st == SSPMV_OK) st = dalloc((unsigned char **)&A.block_data, (size_t)nnzb * A.blockNNZ * sv, s);
+        if (st == SSPMV_OK) {
+            cudaMemsetAsync(A.block_data, 0, (size_t)nnzb * A.blockNNZ * sv, cu(s));
+            if (nnz > 0) {
+                unique_scatter<<<grid_for(nnz, 256, (int64_t)num_sms() * 16), 256, 0, cu(s)>>>(nnz, keys, pos, A.nb,
+                                                                                            ukeys, A.block_colindex);
+                note_launch();
+            }
+            bsr_row_ptr<<<grid_for(A.mb + 1, 256), 256, 0, cu(s)>>>(A.mb, A.nb, nnzb, ukeys, A.row_ptr);
+            note_launch();
+            if (m > 0)
+                st = dispatch_value(vt, [&](auto tag) -> sspmv_status {
+                    using V = decltype(tag);
+                    bsr_fill<V><<<g, 256, 0, cu(s)>>>(m, r, c, csr->row_offset, csr->col_index, (const V *)csr->values,
+                                                      A.row_ptr, A.block_colindex, (V *)A.block_data);
+                    SSPMV_LAUNCH_CHECK();
+                    return SSPMV_OK;
+                });
+            cudaError_t e = cudaStreamSynchronize(cu(s));
+            if (st == SSPMV_OK && e != cudaSuccess) st = fail(SSPMV_CUDA_ERROR, "csr_to_bsr: %s", cudaGetErrorString(e));
+        }
+        dfree(keys, s);
+        dfree(vals, s);
+        dfree(pos, s);
+        dfree(ukeys, s);
+    }
+    if (st != SSPMV_OK) {
+        dfree(A.row_ptr, s);
+        dfree(A.block_colindex, s);
+        dfree(A.block_data, s);
+        return st;
+    }
+    *out = A;
+    return SSPMV_OK;
+}
+
+extern "C" sspmv_status sspmv_spmm_bsr(double alpha, const sspmv_bsr *A, int32_t k, const void *X, int64_t ldx,
+                                       double beta, void *Y, int64_t ldy, sspmv_stream_t s) {
+    if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
+    SSPMV_TRY(check_spmm_args(&A->f, k, X, ldx, Y, ldy));
+    if (A->f.num_rows == 0) return SSPMV_OK;
+    return dispatch_value(A->f.value_type, [&](auto tag) -> sspmv_status {
+        using V = decltype(tag);
+        return for_rhs_chunks<V>(k, (const V *)X, (V *)Y, [&](int32_t step, const V *xs, V *ys) {
+            const V a = (V)alpha, b = (V)beta;
+            switch (step) {
+            case 8: return launch_bsr<V, 8>(A, a, xs, ldx, b, ys, ldy, s);
+            case 4: return launch_bsr<V, 4>(A, a, xs, ldx, b, ys, ldy, s);
+            case 2: return launch_bsr<V, 2>(A, a, xs, ldx, b, ys, ldy, s);
+            default: return launch_bsr<V, 1>(A, a, xs, ldx, b, ys, ldy, s);
+            }
+        });
+    });
+}
+
+extern "C" sspmv_status sspmv_LeSpMV_bsr(double alpha, const sspmv_bsr *A, const void *x, double beta, void *y,
+                                         sspmv_stream_t s) {
+    return sspmv_spmm_bsr(alpha, A, 1, x, 1, beta, y, 1, s);
+}
+
+extern "C" sspmv_status sspmv_bsr_export(const sspmv_bsr *A, int32_t *row_ptr, int32_t *block_colindex,
+                                         void *block_data, sspmv_stream_t s) {
+    if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
+    const bool one = A->blockDim_r == 1 && A->blockDim_c == 1;
+    const size_t nrp = (size_t)(one ? A->f.num_rows : A->mb) + 1;
+    if (row_ptr) SSPMV_CUDA_TRY(cudaMemcpyAsync(row_ptr, A->row_ptr, nrp * 4, cudaMemcpyDeviceToHost, cu(s)));
+    if (block_colindex && A->nnzb)
+        SSPMV_CUDA_TRY(cudaMemcpyAsync(block_colindex, A->block_colindex, (size_t)A->nnzb * 4, cudaMemcpyDeviceToHost, cu(s)));
+    if (block_data && A->nnzb)
+        SSPMV_CUDA_TRY(cudaMemcpyAsync(block_data, A->block_data, (size_t)A->nnzb * A->blockNNZ * vsize(A->f.value_type),
+                                       cudaMemcpyDeviceToHost, cu(s)));
+    SSPMV_CUDA_TRY(cudaStreamSynchronize(cu(s)));
+    return SSPMV_OK;
+}
+
+extern "C" sspmv_status sspmv_delete_bsr(sspmv_bsr *A) {
+    if (!A) return SSPMV_OK;
+    cudaDeviceSynchronize();
+    free_plan(&A->f, nullptr);
+    if (A->f.owns) {
+        dfree(A->row_ptr, nullptr);
+        dfree(A->block_colindex, nullptr);
+        dfree(A->block_data, nullptr);
+    }
+    A->row_ptr = A->block_colindex = nullptr;
+    A->block_data = nullptr;
+    return SSPMV_OK;
+}
+
+extern "C" double sspmv_algorithmic_bytes_bsr(const sspmv_bsr *A, int32_t k, int32_t beta_nonzero) {
+    const double sv = (double)vsize(A->f.value_type);
+    return (double)A->f.num_nnzs * sv + (double)A->nnzb * 4.0 + (double)(A->mb + 1) * 4.0 +
+           (double)k * (double)A->f.num_cols * sv + (double)k * (double)A->f.num_rows * sv * (beta_nonzero ? 2.0 : 1.0);
+}

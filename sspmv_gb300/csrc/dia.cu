@@ -1,0 +1,268 @@
+// dia.cu -- DIA format on sm_103a: GPU converter, SpMV / SpMM, export.
+//
+// Converter (csr_to_dia, include/sparse_conversion.h:612-766): diagonals are
+// numbered in the order a row-major scan first meets them.  On the GPU every
+// diagonal records the smallest CSR position holding it (atomicMin), the
+// occupied diagonals are sorted by that position, and the rank is the
+// diagonal's number -- the same order as the sequential scan.  Values are then
+// written row by row in CSR order, so a duplicated (row, col) keeps its last
+// value as in the reference.  More than max_diags diagonals: SSPMV_INFEASIBLE
+// (the reference exits).  stride = num_rows rounded up to `alignment`.
+//
+// SpMV (LeSpMV_dia, src/spmv_dia.cpp:177-197): one thread per row walks the
+// diagonals: data[d*stride + i] and x[i + offset_d] are both contiguous
+// across a warp, and x is reused from L1/L2 across diagonals.  No atomics
+// (the reference scatters into y with atomics, one OpenMP task per diagonal).
+// Column bound is num_cols (the reference uses num_rows, wrong when not square).
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+#include "plan.cuh"
+#include "primitives.cuh"
+#include "spmv_common.cuh"
+
+namespace sspmv {
+sspmv_status check_dims(int32_t vt, int64_t m, int64_t n, int64_t nnz);
+void init_features(sspmv_features *f, int32_t vt, int64_t m, int64_t n, int64_t nnz, int32_t owns);
+}  // namespace sspmv
+
+using namespace sspmv;
+
+namespace {
+
+constexpr int kBlock = 256;
+
+__global__ void fill_i32(int64_t n, int32_t v, int32_t *__restrict__ p) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+__global__ void dia_first_pos(int64_t m, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
+                              int32_t *__restrict__ first) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        for (int32_t jj = rp[i]; jj < rp[i + 1]; jj++) atomicMin(&first[m - i + ci[jj]], jj);
+}
+
+__global__ void dia_collect(int64_t len, const int32_t *__restrict__ first, int32_t cap,
+                            unsigned long long *__restrict__ count, uint64_t *__restrict__ keys,
+                            uint32_t *__restrict__ vals) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < len; t += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t f = first[t];
+        if (f != 0x7fffffff) {
+            unsigned long long k = atomicAdd(count, 1ull);
+            if (k < (unsigned long long)cap) {
+                keys[k] = (uint64_t)f;
+                vals[k] = (uint32_t)t;
+            }
+        }
+    }
+}
+
+__global__ void dia_rank(int32_t nd, int64_t m, const uint32_t *__restrict__ vals, int32_t *__restrict__ dmap,
+                         int64_t *__restrict__ offsets) {
+    int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < nd) {
+        dmap[vals[r]] = r;
+        offsets[r] = (int64_t)vals[r] - m;
+    }
+}
+
+template <typename V>
+__global__ void dia_fill(int64_t m, int64_t stride, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
+                         const V *__restrict__ cv, const int32_t *__restrict__ dmap, V *__restrict__ data) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        for (int32_t jj = rp[i]; jj < rp[i + 1]; jj++) data[(int64_t)dmap[m - i + ci[jj]] * stride + i] = cv[jj];
+}
+
+template <typename V, int K>
+__global__ void __launch_bounds__(kBlock) dia_spmv_kernel(int m, int n, int nd, int64_t stride,
+                                                        const int64_t *__restrict__ offsets,
+                                                        const V *__restrict__ data, const V *__restrict__ x,
+                                                        int64_t ldx, V alpha, V beta, V *__restrict__ y,
+                                                        int64_t ldy) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        V s[K];
+#pragma unroll
+        for (int q = 0; q < K; q++) s[q] = V(0);
+        int d = 0;
+        for (; d + 4 <= nd; d += 4) {
+            int64_t j[4];
+            V a[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                j[u] = i + __ldg(offsets + d + u);
+                a[u] = (j[u] >= 0 && j[u] < n) ? ld_stream(data + (int64_t)(d + u) * stride + i) : V(0);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (j[u] >= 0 && j[u] < n) {
+#pragma unroll
+                    for (int q = 0; q < K; q++) s[q] += a[u] * ld_x(x + j[u] * ldx + q);
+                }
+        }
+        for (; d < nd; d++) {
+            const int64_t j = i + __ldg(offsets + d);
+            if (j >= 0 && j < n) {
+                const V a = ld_stream(data + (int64_t)d * stride + i);
+#pragma unroll
+                for (int q = 0; q < K; q++) s[q] += a * ld_x(x + j * ldx + q);
+            }
+        }
+        V *yp = y + i * ldy;
+#pragma unroll
+        for (int q = 0; q < K; q++) yp[q] = axpby(alpha, s[q], beta, yp + q);
+    }
+}
+
+template <typename V, int K>
+sspmv_status launch_dia(const sspmv_dia *A, V alpha, const V *x, int64_t ldx, V beta, V *y, int64_t ldy,
+                        sspmv_stream_t s) {
+    const unsigned grid = grid_for(A->f.num_rows, kBlock, (int64_t)num_sms() * 16);
+    dia_spmv_kernel<V, K><<<grid, kBlock, 0, cu(s)>>>((int)A->f.num_rows, (int)A->f.num_cols, A->complete_ndiags,
+                                                      A->stride, A->diag_offsets, (const V *)A->diag_data, x, ldx,
+                                                      alpha, beta, y, ldy);
+    SSPMV_LAUNCH_CHECK();
+    return SSPMV_OK;
+}
+
+}  // namespace
+
+extern "C" sspmv_status sspmv_csr_to_dia(const sspmv_csr *csr, int32_t max_diags, int32_t align, sspmv_dia *out,
+                                         sspmv_stream_t s) {
+    if (!csr || !out) return fail(SSPMV_INVALID_ARG, "null argument");
+    SSPMV_TRY(check_dims(csr->f.value_type, csr->f.num_rows, csr->f.num_cols, csr->f.num_nnzs));
+    if (max_diags == 0) max_diags = 10240;
+    if (align == 0) align = default_alignment(csr->f.value_type);
+    if (max_diags < 0 || align < 1) return fail(SSPMV_INVALID_ARG, "max_diags >= 0 and alignment >= 1 required");
+    const int64_t m = csr->f.num_rows, n = csr->f.num_cols, len = m + n;
+    const int32_t vt = csr->f.value_type;
+    int32_t *first = nullptr, *dmap = nullptr;
+    uint64_t *keys = nullptr;
+    uint32_t *vals = nullptr;
+    unsigned long long *d_count = nullptr;
+    sspmv_dia A;
+    init_features(&A.f, vt, m, n, csr->f.num_nnzs, 1);
+    A.diag_offsets = nullptr;
+    A.diag_data = nullptr;
+    auto cleanup = [&]() {
+        dfree(first, s);
+        dfree(dmap, s);
+        dfree(keys, s);
+        dfree(vals, s);
+        dfree(d_count, s);
+    };
+    const unsigned g = grid_for(std::max<int64_t>(m, 1), 256, (int64_t)num_sms() * 16);
+    const unsigned gl = grid_for(std::max<int64_t>(len, 1), 256, (int64_t)num_sms() * 16);
+    sspmv_status st = dalloc(&first, (size_t)len, s);
+    if (st == SSPMV_OK) st = dalloc(&keys, (size_t)max_diags + 1, s);
+    if (st == SSPMV_OK) st = dalloc(&vals, (size_t)max_diags + 1, s);
+    if (st == SSPMV_OK) st = dalloc(&d_count, 1, s);
+    unsigned long long count = 0;
+    if (st == SSPMV_OK && len > 0) {
+        fill_i32<<<gl, 256, 0, cu(s)>>>(len, 0x7fffffff, first);
+        note_launch();
+        cudaMemsetAsync(d_count, 0, 8, cu(s));
+        if (m > 0) {
+            dia_first_pos<<<g, 256, 0, cu(s)>>>(m, csr->row_offset, csr->col_index, first);
+            note_launch();
+        }
+        dia_collect<<<gl, 256, 0, cu(s)>>>(len, first, max_diags + 1, d_count, keys, vals);
+        note_launch();
+        cudaError_t e = cudaMemcpyAsync(&count, d_count, 8, cudaMemcpyDeviceToHost, cu(s));
+        if (e == cudaSuccess) e = cudaStreamSynchronize(cu(s));
+        if (e != cudaSuccess) st = fail(SSPMV_CUDA_ERROR, "csr_to_dia: %s", cudaGetErrorString(e));
+    }
+    if (st == SSPMV_OK && count > (unsigned long long)max_diags)
+        st = fail(SSPMV_INFEASIBLE, "number of diagonals (%llu) exceeds limit (%d)", count, max_diags);
+    const int32_t nd = (int32_t)count;
+    const int64_t stride = (int64_t)align * ((m + align - 1) / align);
+    if (st == SSPMV_OK) st = radix_sort_pairs(keys, vals, nd, bits_for((uint64_t)std::max<int64_t>(csr->f.num_nnzs, 1)), s);
+    if (st == SSPMV_OK) st = dalloc(&dmap, (size_t)len, s);
+    if (st == SSPMV_OK) st = dalloc(&A.diag_offsets, (size_t)nd, s);
+    if (st == SSPMV_OK) st = dalloc((unsigned char **)&A.diag_data, (size_t)nd * stride * vsize(vt), s);
+    if (st == SSPMV_OK) {
+        cudaMemsetAsync(A.diag_data, 0, (size_t)nd * stride * vsize(vt), cu(s));
+        if (nd > 0) {
+            dia_rank<<<grid_for(nd, 256), 256, 0, cu(s)>>>(nd, m, vals, dmap, A.diag_offsets);
+            note_launch();
+        }
+        if (m > 0) {
+            st = dispatch_value(vt, [&](auto tag) -> sspmv_status {
+                using V = decltype(tag);
+                dia_fill<V><<<g, 256, 0, cu(s)>>>(m, stride, csr->row_offset, csr->col_index, (const V *)csr->values,
+                                                  dmap, (V *)A.diag_data);
+                SSPMV_LAUNCH_CHECK();
+                return SSPMV_OK;
+            });
+        }
+        cudaError_t e = cudaStreamSynchronize(cu(s));
+        if (st == SSPMV_OK && e != cudaSuccess) st = fail(SSPMV_CUDA_ERROR, "csr_to_dia: %s", cudaGetErrorString(e));
+    }
+    cleanup();
+    if (st != SSPMV_OK) {
+        dfree(A.diag_offsets, s);
+        dfree(A.diag_data, s);
+        return st;
+    }
+    A.stride = (int32_t)stride;
+    A.complete_ndiags = nd;
+    *out = A;
+    return SSPMV_OK;
+}
+
+extern "C" sspmv_status sspmv_spmm_dia(double alpha, const sspmv_dia *A, int32_t k, const void *X, int64_t ldx,
+                                       double beta, void *Y, int64_t ldy, sspmv_stream_t s) {
+    if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
+    SSPMV_TRY(check_spmm_args(&A->f, k, X, ldx, Y, ldy));
+    if (A->f.num_rows == 0) return SSPMV_OK;
+    return dispatch_value(A->f.value_type, [&](auto tag) -> sspmv_status {
+        using V = decltype(tag);
+        return for_rhs_chunks<V>(k, (const V *)X, (V *)Y, [&](int32_t step, const V *xs, V *ys) {
+            const V a = (V)alpha, b = (V)beta;
+            switch (step) {
+            case 8: return launch_dia<V, 8>(A, a, xs, ldx, b, ys, ldy, s);
+            case 4: return launch_dia<V, 4>(A, a, xs, ldx, b, ys, ldy, s);
+            case 2: return launch_dia<V, 2>(A, a, xs, ldx, b, ys, ldy, s);
+            default: return launch_dia<V, 1>(A, a, xs, ldx, b, ys, ldy, s);
+            }
+        });
+    });
+}
+
+extern "C" sspmv_status sspmv_LeSpMV_dia(double alpha, const sspmv_dia *A, const void *x, double beta, void *y,
+                                         sspmv_stream_t s) {
+    return sspmv_spmm_dia(alpha, A, 1, x, 1, beta, y, 1, s);
+}
+
+extern "C" sspmv_status sspmv_dia_export(const sspmv_dia *A, int64_t *diag_offsets, void *diag_data,
+                                         sspmv_stream_t s) {
+    if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
+    const size_t nd = (size_t)A->complete_ndiags;
+    if (diag_offsets && nd)
+        SSPMV_CUDA_TRY(cudaMemcpyAsync(diag_offsets, A->diag_offsets, nd * 8, cudaMemcpyDeviceToHost, cu(s)));
+    if (diag_data && nd)
+        SSPMV_CUDA_TRY(cudaMemcpyAsync(diag_data, A->diag_data, nd * (size_t)A->stride * vsize(A->f.value_type),
+                                       cudaMemcpyDeviceToHost, cu(s)));
+    SSPMV_CUDA_TRY(cudaStreamSynchronize(cu(s)));
+    return SSPMV_OK;
+}
+
+extern "C" sspmv_status sspmv_delete_dia(sspmv_dia *A) {
+    if (!A) return SSPMV_OK;
+    cudaDeviceSynchronize();
+    free_plan(&A->f, nullptr);
+    if (A->f.owns) {
+        dfree(A->diag_offsets, nullptr);
+        dfree(A->diag_data, nullptr);
+    }
+    A->diag_offsets = nullptr;
+    A->diag_data = nullptr;
+    return SSPMV_OK;
+}
+
+extern "C" double sspmv_algorithmic_bytes_dia(const sspmv_dia *A, int32_t k, int32_t beta_nonzero) {
+    const double sv = (double)vsize(A->f.value_type);
+    return (double)A->f.num_nnzs * sv + (double)A->complete_ndiags * 8.0 + (double)k * (double)A->f.num_cols * sv +
+           (double)k * (double)A->f.num_rows * sv * (beta_nonzero ? 2.0 : 1.0);
+}

@@ -158,6 +158,81 @@ class SELL_C_R_Matrix(_SellReordered):
     fmt = "sell_c_R"
 
 
+class COO_Matrix(Matrix):
+    fmt = "coo"
+
+    def export(self, stream=None) -> dict:
+        ri, pr = _host(self.num_nnzs, np.int32)
+        ci, pc = _host(self.num_nnzs, np.int32)
+        v, pv = _host(self.num_nnzs, self.dtype)
+        call("sspmv_coo_export", self.ref(), pr, pc, pv, _stream(stream))
+        return {"row": ri, "col": ci, "val": v}
+
+
+class DIA_Matrix(Matrix):
+    fmt = "dia"
+
+    def export(self, stream=None) -> dict:
+        nd, st = int(self.s.complete_ndiags), int(self.s.stride)
+        off, po = _host(nd, np.int64)
+        data, pd = _host(nd * st, self.dtype)
+        call("sspmv_dia_export", self.ref(), po, pd, _stream(stream))
+        return {"complete_ndiags": nd, "stride": st, "offsets": off, "data": data}
+
+
+class BSR_Matrix(Matrix):
+    fmt = "bsr"
+
+    def export(self, stream=None) -> dict:
+        s = self.s
+        one = s.blockDim_r == 1 and s.blockDim_c == 1
+        rp, prp = _host((self.num_rows if one else s.mb) + 1, np.int32)
+        ci, pci = _host(s.nnzb, np.int32)
+        data, pd = _host(s.nnzb * s.blockNNZ, self.dtype)
+        call("sspmv_bsr_export", self.ref(), prp, pci, pd, _stream(stream))
+        return {"mb": int(s.mb), "nb": int(s.nb), "nnzb": int(s.nnzb), "row_ptr": rp, "colindex": ci,
+                "data": data, "r": int(s.blockDim_r), "c": int(s.blockDim_c)}
+
+
+def csr_to_coo(csr: CSR_Matrix, stream=None) -> COO_Matrix:
+    """csr_to_coo (include/sparse_conversion.h:145-168)."""
+    s = _lib.Coo()
+    call("sspmv_csr_to_coo", csr.ref(), C.byref(s), _stream(stream))
+    return COO_Matrix(s)
+
+
+def coo_from_host(num_rows, num_cols, row_index, col_index, values, stream=None) -> COO_Matrix:
+    s = _lib.Coo()
+    v = np.ascontiguousarray(values)
+    ri = np.ascontiguousarray(row_index, np.int32)
+    ci = np.ascontiguousarray(col_index, np.int32)
+    call("sspmv_coo_create", C.byref(s), _vt(v.dtype), num_rows, num_cols, len(v), ri.ctypes.data_as(C.c_void_p),
+         ci.ctypes.data_as(C.c_void_p), v.ctypes.data_as(C.c_void_p), 1, _stream(stream))
+    return COO_Matrix(s)
+
+
+def coo_to_csr(coo: COO_Matrix, stream=None) -> CSR_Matrix:
+    """coo_to_csr (include/sparse_conversion.h:30-91, compact = false)."""
+    s = Csr()
+    call("sspmv_coo_to_csr", coo.ref(), C.byref(s), _stream(stream))
+    return CSR_Matrix(s)
+
+
+def csr_to_dia(csr: CSR_Matrix, max_diags: int = 0, alignment: int = 0, stream=None) -> DIA_Matrix:
+    """csr_to_dia (include/sparse_conversion.h:612-766); SSPMVError status 2
+    (SSPMV_INFEASIBLE) above max_diags."""
+    s = _lib.Dia()
+    call("sspmv_csr_to_dia", csr.ref(), int(max_diags), int(alignment), C.byref(s), _stream(stream))
+    return DIA_Matrix(s)
+
+
+def csr_to_bsr(csr: CSR_Matrix, blockDimRow: int = 0, blockDimCol: int = 0, stream=None) -> BSR_Matrix:
+    """csr_to_bsr (include/sparse_conversion.h:769-926); 0 = reference default."""
+    s = _lib.Bsr()
+    call("sspmv_csr_to_bsr", csr.ref(), int(blockDimRow), int(blockDimCol), C.byref(s), _stream(stream))
+    return BSR_Matrix(s)
+
+
 def csr_to_ell(csr: CSR_Matrix, ld: int = RowMajor, stream=None) -> ELL_Matrix:
     """csr_to_ell (include/sparse_conversion.h:187-248)."""
     s = _lib.Ell()
@@ -238,9 +313,9 @@ def LeSpMV_csr(alpha, A: CSR_Matrix, x, beta, y, stream=None) -> None:
 
 
 # Formats the library builds, in benchmark order.
-FORMATS = ["csr", "ell", "sell", "sell_c_sigma", "sell_c_R"]
+FORMATS = ["csr", "coo", "ell", "sell", "sell_c_sigma", "sell_c_R", "dia", "bsr"]
 # Formats the smoke check converts from CSR (besides CSR itself).
-SMOKE_FORMATS: list[str] = ["ell", "sell", "sell_c_sigma", "sell_c_R"]
+SMOKE_FORMATS: list[str] = ["coo", "ell", "sell", "sell_c_sigma", "sell_c_R", "bsr"]
 
 
 def bsr_block_for(A: HostCSR) -> tuple[int, int]:
