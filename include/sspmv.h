@@ -181,6 +181,27 @@ typedef struct {
     void *block_data;        /* [nnzb * blockNNZ] */
 } sspmv_bsr;
 
+/* CSR5_Matrix (include/sparse_format.h:141-166): the CSR arrays (col_index /
+ * values transposed tile by tile) plus the tile pointer and descriptors. */
+typedef struct {
+    sspmv_features f;
+    int32_t *row_offset;
+    int32_t *col_index;
+    void *values;
+    int32_t sigma;
+    int32_t omega;
+    int32_t bit_y_offset;
+    int32_t bit_scansum_offset;
+    int32_t num_packets;
+    int32_t num_offsets;
+    int32_t _p;
+    int32_t tail_partition_start;
+    uint32_t *tile_ptr;             /* [_p + 1] */
+    uint32_t *tile_desc;            /* [_p * omega * num_packets] */
+    int32_t *tile_desc_offset_ptr;  /* [_p + 1] */
+    int32_t *tile_desc_offset;      /* [num_offsets] */
+} sspmv_csr5;
+
 /* ---------------- status / memory ---------------- */
 const char *sspmv_status_string(sspmv_status s);
 const char *sspmv_last_error(void);
@@ -311,6 +332,10 @@ sspmv_status sspmv_delete_dia(sspmv_dia *A);
  * (16 x 64/sizeof(value)). */
 sspmv_status sspmv_csr_to_bsr(const sspmv_csr *csr, int32_t blockDimRow, int32_t blockDimCol, sspmv_bsr *out,
                               sspmv_stream_t stream);
+/* Number of distinct r x c blocks csr_to_bsr would make (no block data is
+ * allocated): lets a caller bound the fill before converting. */
+sspmv_status sspmv_csr_count_blocks(const sspmv_csr *csr, int32_t blockDimRow, int32_t blockDimCol, int64_t *nnzb,
+                                    sspmv_stream_t stream);
 /* LeSpMV_bsr (src/spmv_bsr.cpp:215-233) */
 sspmv_status sspmv_LeSpMV_bsr(double alpha, const sspmv_bsr *A, const void *x, double beta, void *y,
                               sspmv_stream_t stream);
@@ -322,9 +347,27 @@ sspmv_status sspmv_bsr_export(const sspmv_bsr *A, int32_t *row_ptr, int32_t *blo
                               sspmv_stream_t stream);
 sspmv_status sspmv_delete_bsr(sspmv_bsr *A);
 
+/* ---------------- CSR5 ---------------- */
+/* csr_to_csr5 (include/sparse_conversion.h:939-1379); sigma / omega 0 =
+ * reference defaults (16, 64/sizeof(value)); the SpMV kernel accepts omega in
+ * {4, 8, 16, 32}. */
+sspmv_status sspmv_csr_to_csr5(const sspmv_csr *csr, int32_t sigma, int32_t omega, sspmv_csr5 *out,
+                               sspmv_stream_t stream);
+/* LeSpMV_csr5 (src/spmv_csr5.cpp:439-457) */
+sspmv_status sspmv_LeSpMV_csr5(double alpha, const sspmv_csr5 *A, const void *x, double beta, void *y,
+                               sspmv_stream_t stream);
+sspmv_status sspmv_spmm_csr5(double alpha, const sspmv_csr5 *A, int32_t k, const void *X, int64_t ldx,
+                             double beta, void *Y, int64_t ldy, sspmv_stream_t stream);
+/* Sizes from the struct fields; col_index / values are the transposed copies. */
+sspmv_status sspmv_csr5_export(const sspmv_csr5 *A, uint32_t *tile_ptr, uint32_t *tile_desc,
+                               int32_t *tile_desc_offset_ptr, int32_t *tile_desc_offset, int32_t *col_index,
+                               void *values, sspmv_stream_t stream);
+sspmv_status sspmv_delete_csr5(sspmv_csr5 *A);
+
 /* Algorithmic bytes of one SpMV with k right-hand sides: structural bytes of
  * the format (padding excluded) + x once + y once (twice when beta != 0). */
 double sspmv_algorithmic_bytes_csr(const sspmv_csr *A, int32_t k, int32_t beta_nonzero);
+double sspmv_algorithmic_bytes_csr5(const sspmv_csr5 *A, int32_t k, int32_t beta_nonzero);
 double sspmv_algorithmic_bytes_coo(const sspmv_coo *A, int32_t k, int32_t beta_nonzero);
 double sspmv_algorithmic_bytes_dia(const sspmv_dia *A, int32_t k, int32_t beta_nonzero);
 double sspmv_algorithmic_bytes_bsr(const sspmv_bsr *A, int32_t k, int32_t beta_nonzero);

@@ -82,6 +82,17 @@ class Bsr(C.Structure):
                 ("block_colindex", P32), ("block_data", C.c_void_p)]
 
 
+PU32 = C.POINTER(C.c_uint32)
+
+
+class Csr5(C.Structure):
+    _fields_ = [("f", Features), ("row_offset", P32), ("col_index", P32), ("values", C.c_void_p),
+                ("sigma", C.c_int32), ("omega", C.c_int32), ("bit_y_offset", C.c_int32),
+                ("bit_scansum_offset", C.c_int32), ("num_packets", C.c_int32), ("num_offsets", C.c_int32),
+                ("_p", C.c_int32), ("tail_partition_start", C.c_int32), ("tile_ptr", PU32), ("tile_desc", PU32),
+                ("tile_desc_offset_ptr", P32), ("tile_desc_offset", P32)]
+
+
 class SynthParams(C.Structure):
     _fields_ = [("family", C.c_int32), ("num_offsets", C.c_int32), ("num_rows", C.c_int64),
                 ("num_cols", C.c_int64), ("grid", C.c_int64), ("offsets", C.c_int64 * 32),
@@ -155,8 +166,10 @@ _SIGS.update(_format_sigs("sell_c_R", SellCR, [_i32, _i32], [_vp, _vp, _vp, _vp]
 _SIGS.update(_format_sigs("coo", Coo, [], [_vp, _vp, _vp]))
 _SIGS.update(_format_sigs("dia", Dia, [_i32, _i32], [_vp, _vp]))
 _SIGS.update(_format_sigs("bsr", Bsr, [_i32, _i32], [_vp, _vp, _vp]))
+_SIGS.update(_format_sigs("csr5", Csr5, [_i32, _i32], [_vp, _vp, _vp, _vp, _vp, _vp]))
 _SIGS["sspmv_coo_create"] = (_st, [C.POINTER(Coo), _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp])
 _SIGS["sspmv_coo_to_csr"] = (_st, [C.POINTER(Coo), C.POINTER(Csr), _vp])
+_SIGS["sspmv_csr_count_blocks"] = (_st, [C.POINTER(Csr), _i32, _i32, C.POINTER(_i64), _vp])
 
 for _n, (_r, _a) in _SIGS.items():
     register(_n, _r, _a)

@@ -253,6 +253,39 @@ extern "C" sspmv_status sspmv_csr_to_bsr(const sspmv_csr *csr, int32_t r, int32_
     return SSPMV_OK;
 }
 
+extern "C" sspmv_status sspmv_csr_count_blocks(const sspmv_csr *csr, int32_t r, int32_t c, int64_t *nnzb,
+                                               sspmv_stream_t s) {
+    if (!csr || !nnzb) return fail(SSPMV_INVALID_ARG, "null argument");
+    if (r < 1 || c < 1) return fail(SSPMV_INVALID_ARG, "block dimensions must be >= 1");
+    const int64_t m = csr->f.num_rows, n = csr->f.num_cols, nnz = csr->f.num_nnzs;
+    *nnzb = 0;
+    if (nnz == 0) return SSPMV_OK;
+    const int64_t mb = (m + r - 1) / r, nb = (n + c - 1) / c;
+    uint64_t *keys = nullptr;
+    uint32_t *vals = nullptr;
+    int32_t *pos = nullptr;
+    sspmv_status st = dalloc(&keys, (size_t)nnz, s);
+    if (st == SSPMV_OK) st = dalloc(&vals, (size_t)nnz, s);
+    if (st == SSPMV_OK) st = dalloc(&pos, (size_t)nnz, s);
+    if (st == SSPMV_OK) {
+        bsr_keys<<<grid_for(m, 256, (int64_t)num_sms() * 16), 256, 0, cu(s)>>>(m, r, c, nb, csr->row_offset,
+                                                                                csr->col_index, keys, vals);
+        note_launch();
+        st = radix_sort_pairs(keys, vals, nnz, bits_for((uint64_t)(mb * nb)), s);
+    }
+    int32_t total = 0;
+    if (st == SSPMV_OK) {
+        unique_flags<<<grid_for(nnz, 256, (int64_t)num_sms() * 16), 256, 0, cu(s)>>>(nnz, keys, pos);
+        note_launch();
+        st = exclusive_scan_i32(pos, pos, nnz, &total, s);
+    }
+    dfree(keys, s);
+    dfree(vals, s);
+    dfree(pos, s);
+    if (st == SSPMV_OK) *nnzb = total;
+    return st;
+}
+
 extern "C" sspmv_status sspmv_spmm_bsr(double alpha, const sspmv_bsr *A, int32_t k, const void *X, int64_t ldx,
                                        double beta, void *Y, int64_t ldy, sspmv_stream_t s) {
     if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");

@@ -194,6 +194,33 @@ class BSR_Matrix(Matrix):
                 "data": data, "r": int(s.blockDim_r), "c": int(s.blockDim_c)}
 
 
+class CSR5_Matrix(Matrix):
+    fmt = "csr5"
+
+    def export(self, stream=None) -> dict:
+        s = self.s
+        p = int(s._p)
+        tp, ptp = _host(p + 1, np.uint32)
+        td, ptd = _host(p * s.omega * s.num_packets, np.uint32)
+        tdp, ptdp = _host(p + 1, np.int32)
+        tdo, ptdo = _host(s.num_offsets, np.int32)
+        col, pc = _host(self.num_nnzs, np.int32)
+        val, pv = _host(self.num_nnzs, self.dtype)
+        call("sspmv_csr5_export", self.ref(), ptp, ptd, ptdp, ptdo, pc, pv, _stream(stream))
+        return {"sigma": int(s.sigma), "omega": int(s.omega), "bit_y_offset": int(s.bit_y_offset),
+                "bit_scansum_offset": int(s.bit_scansum_offset), "num_packets": int(s.num_packets), "p": p,
+                "num_offsets": int(s.num_offsets), "tail_partition_start": int(s.tail_partition_start),
+                "tile_ptr": tp, "tile_desc": td, "tile_desc_offset_ptr": tdp, "tile_desc_offset": tdo,
+                "col": col, "val": val}
+
+
+def csr_to_csr5(csr: CSR_Matrix, sigma: int = 0, omega: int = 0, stream=None) -> CSR5_Matrix:
+    """csr_to_csr5 (include/sparse_conversion.h:939-1379); 0 = reference default."""
+    s = _lib.Csr5()
+    call("sspmv_csr_to_csr5", csr.ref(), int(sigma), int(omega), C.byref(s), _stream(stream))
+    return CSR5_Matrix(s)
+
+
 def csr_to_coo(csr: CSR_Matrix, stream=None) -> COO_Matrix:
     """csr_to_coo (include/sparse_conversion.h:145-168)."""
     s = _lib.Coo()
@@ -313,9 +340,9 @@ def LeSpMV_csr(alpha, A: CSR_Matrix, x, beta, y, stream=None) -> None:
 
 
 # Formats the library builds, in benchmark order.
-FORMATS = ["csr", "coo", "ell", "sell", "sell_c_sigma", "sell_c_R", "dia", "bsr"]
+FORMATS = ["csr", "coo", "ell", "sell", "sell_c_sigma", "sell_c_R", "dia", "bsr", "csr5"]
 # Formats the smoke check converts from CSR (besides CSR itself).
-SMOKE_FORMATS: list[str] = ["coo", "ell", "sell", "sell_c_sigma", "sell_c_R", "bsr"]
+SMOKE_FORMATS: list[str] = ["coo", "ell", "sell", "sell_c_sigma", "sell_c_R", "bsr", "csr5"]
 
 
 def bsr_block_for(A: HostCSR) -> tuple[int, int]:
@@ -335,7 +362,7 @@ def feasible_host(fmt: str, A: HostCSR) -> tuple[bool, str]:
         return (m * w <= 4 * nnz, f"ELL width {w} pads {m * w / nnz:.1f}x")
     if fmt == "dia":
         rows = np.repeat(np.arange(m, dtype=np.int64), lens)
-        nd = len(np.unique(A.col_index.astype(np.int64) - rows))
+        nd = int(np.count_nonzero(np.bincount(A.col_index.astype(np.int64) - rows + m, minlength=1)))
         return (nd <= 10240, f"{nd} diagonals > 10240")
     if fmt == "bsr":
         r, c = bsr_block_for(A)
@@ -346,12 +373,26 @@ def feasible_host(fmt: str, A: HostCSR) -> tuple[bool, str]:
     return False, "unknown format"
 
 
+def count_blocks(csr: CSR_Matrix, r: int, c: int, stream=None) -> int:
+    """Distinct r x c blocks of a device CSR (no block data allocated)."""
+    n = C.c_int64()
+    call("sspmv_csr_count_blocks", csr.ref(), int(r), int(c), C.byref(n), _stream(stream))
+    return int(n.value)
+
+
 def build_format(csr: CSR_Matrix, fmt: str, A: HostCSR | None = None):
-    """Converts a device CSR to `fmt`; returns (matrix, None) or (None, why)."""
-    if A is not None:
+    """Converts a device CSR to `fmt`; returns (matrix, None) or (None, why).
+    Formats whose padding or block fill exceeds 4x the CSR size are skipped;
+    DIA over 10240 diagonals is reported by the converter itself."""
+    if fmt == "ell" and A is not None:
         ok, why = feasible_host(fmt, A)
         if not ok:
             return None, why
+    if fmt == "bsr":
+        r, c = bsr_block_for(A) if A is not None else (4, 4)
+        nnzb = count_blocks(csr, r, c)
+        if nnzb * r * c > 4 * max(csr.num_nnzs, 1):
+            return None, f"BSR {r}x{c} fill {nnzb * r * c / max(csr.num_nnzs, 1):.1f}x"
     if fmt == "csr":
         return csr, None
     fn = globals().get(f"csr_to_{fmt}")

@@ -112,6 +112,9 @@ ORACLE_CONV = {
     "bsr4x4": lambda O, A: O.csr_to_bsr(A, 4, 4),
     "bsr2x8": lambda O, A: O.csr_to_bsr(A, 2, 8),
     "bsr3x5": lambda O, A: O.csr_to_bsr(A, 3, 5),
+    "csr5": lambda O, A: O.csr_to_csr5(A),
+    "csr5_w32": lambda O, A: O.csr_to_csr5(A, 16, 32),
+    "csr5_s12_w4": lambda O, A: O.csr_to_csr5(A, 12, 4),
 }
 GPU_CONV = {
     "ell": lambda L, M: L.csr_to_ell(M, 0),
@@ -123,6 +126,9 @@ GPU_CONV = {
     "bsr4x4": lambda L, M: L.csr_to_bsr(M, 4, 4),
     "bsr2x8": lambda L, M: L.csr_to_bsr(M, 2, 8),
     "bsr3x5": lambda L, M: L.csr_to_bsr(M, 3, 5),
+    "csr5": lambda L, M: L.csr_to_csr5(M),
+    "csr5_w32": lambda L, M: L.csr_to_csr5(M, 16, 32),
+    "csr5_s12_w4": lambda L, M: L.csr_to_csr5(M, 12, 4),
 }
 
 
