@@ -54,6 +54,14 @@ def parse_args():
     return ap.parse_args()
 
 
+_T0 = time.perf_counter()
+
+
+def log(msg: str) -> None:
+    """Progress line on stderr (stdout carries only the JSON result)."""
+    print(f"[bench {time.perf_counter() - _T0:7.1f}s] {msg}", file=sys.stderr, flush=True)
+
+
 def np_dtype(tag):
     return np.float64 if tag == "f64" else np.float32
 
@@ -147,6 +155,7 @@ def run_gpu(args, rank, world):
     dtypes = [d for d in args.dtypes.split(",") if d]
     fmts = L.FORMATS if args.formats == "all" else args.formats.split(",")
     hosts = host_matrices(families, args.scale)
+    log("host matrices generated")
 
     cases, skipped = [], []
     for fam in families:
@@ -154,7 +163,10 @@ def run_gpu(args, rank, world):
             A = hosts[(fam, dt)]
             csr = L.csr_from_host(A)
             for fmt in fmts:
+                t_conv = time.perf_counter()
                 M, why = L.build_format(csr, fmt, A)
+                log(f"convert {fam}/{fmt}/{dt}: {'skipped' if M is None else 'ok'} "
+                    f"({time.perf_counter() - t_conv:.2f}s)")
                 if M is None:
                     skipped.append(f"{fam}/{fmt}/{dt}: {why}")
                     continue
@@ -177,6 +189,7 @@ def run_gpu(args, rank, world):
     for c in cases:
         c.setdefault("tuned", None)
         c["kernel"] = {"kernel_flag": c["M"].kernel_flag}
+    log("tuned")
 
     def one_step(record):
         for c in cases:
@@ -210,6 +223,7 @@ def run_gpu(args, rank, world):
     launches = _lib.lib.sspmv_launch_count() - launches0
     clocks = sampler.stop()
     _barrier(world)
+    log("timed steps done")
 
     per_case = []
     total_ms = 0.0
@@ -230,6 +244,7 @@ def run_gpu(args, rank, world):
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(args, cases, flush, stream, world)
+        log("e2e done")
 
     dom = max(range(len(cases)), key=lambda i: per_case[i]["ms"])
     dc = cases[dom]
@@ -244,6 +259,7 @@ def run_gpu(args, rank, world):
     cpu = None
     if rank == 0 and world == 1:
         cpu = cpu_baseline(hosts, families, dtypes, fmts, budget_s=15.0)
+        log("cpu baseline done")
     return {
         "metric": "SpMV GB/s (algorithmic bytes / kernel time), all formats x 4 families x {f64,f32}",
         "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,

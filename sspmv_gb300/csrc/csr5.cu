@@ -253,9 +253,11 @@ __global__ void __launch_bounds__(kBlock) csr5_tile_kernel(C5View A, const V *__
     const int32_t row_start = (int32_t)(tp0 & 0x7FFFFFFFu);
     const uint32_t *dl = A.td + (size_t)t * OMEGA * A.np;
     const int32_t optr = (active && dirty) ? A.tdo_ptr[t] : 0;
+    // segment rel >= 1 of a tile with empty rows: tile_desc_offset holds its
+    // row counted from row_start + 1 (include/sparse_conversion.h:1290-1305)
     auto map_row = [&](int32_t rel) -> int64_t {
         if (rel == 0) return row_start;
-        return (int64_t)row_start + (dirty ? A.tdo[optr + rel - 1] : rel);
+        return (int64_t)row_start + (dirty ? 1 + A.tdo[optr + rel - 1] : rel);
     };
 
     V sum[K], head[K];

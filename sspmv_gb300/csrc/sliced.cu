@@ -38,16 +38,24 @@ namespace {
 constexpr int kBlock = 256;
 
 // ------------------------------------------------------------------ SpMV --
+// Chunks wider than kLongWidth slots are not handled a thread per row (a
+// 38k-slot row would serialise its warp): they are cut into pieces of about
+// kPieceElems slab elements, each read by one warp with consecutive lanes on
+// consecutive slab elements, and a fix-up adds a chunk's pieces in order.
+constexpr int64_t kLongWidth = 64;
+constexpr int64_t kPieceElems = 2048;
+
 template <typename V, int K>
 __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
     int m, int C, const int64_t *__restrict__ chunk_ptr, const int32_t *__restrict__ reorder,
     const int32_t *__restrict__ col, const V *__restrict__ val, const V *__restrict__ x, int64_t ldx, V alpha,
-    V beta, V *__restrict__ y, int64_t ldy) {
+    V beta, V *__restrict__ y, int64_t ldy, int64_t long_width) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t c = i / C;
         const int r = (int)(i - c * C);
         const int64_t base = ld_stream(chunk_ptr + c);
         const int64_t w = (ld_stream(chunk_ptr + c + 1) - base) / C;
+        if (w > long_width) continue;  // pieces kernel
         const int32_t *cp = col + base + r;
         const V *vp = val + base + r;
         V s[K];
@@ -86,6 +94,100 @@ __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
     }
 }
 
+// piece = {chunk, first slot, end slot}; one warp per piece
+template <typename V, int K>
+__global__ void __launch_bounds__(kBlock) sliced_piece_kernel(
+    int64_t npieces, int C, const int4 *__restrict__ pieces, const int64_t *__restrict__ chunk_ptr,
+    const int32_t *__restrict__ col, const V *__restrict__ val, const V *__restrict__ x, int64_t ldx,
+    V *__restrict__ partial) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp >= npieces) return;
+    const int4 pc = pieces[warp];
+    const int64_t base = chunk_ptr[pc.x];
+    V *out = partial + warp * (int64_t)C * kMaxK;
+    if (32 % C == 0) {
+        // lane -> (row lane % C, slot lane / C): a warp step reads 32
+        // consecutive slab elements
+        const int r = lane % C, sl = lane / C, step = 32 / C;
+        V s[K];
+#pragma unroll
+        for (int q = 0; q < K; q++) s[q] = V(0);
+        int64_t k = pc.y + sl;
+        for (; k + 3 * step < pc.z; k += 4 * step) {
+            int cc[4];
+            V aa[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int64_t idx = base + (k + u * step) * C + r;
+                cc[u] = ld_stream(col + idx);
+                aa[u] = ld_stream(val + idx);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (cc[u] >= 0) {
+#pragma unroll
+                    for (int q = 0; q < K; q++) s[q] += aa[u] * ld_x(x + (int64_t)cc[u] * ldx + q);
+                }
+        }
+        for (; k < pc.z; k += step) {
+            const int64_t idx = base + k * C + r;
+            const int cc = ld_stream(col + idx);
+            if (cc >= 0) {
+                const V aa = ld_stream(val + idx);
+#pragma unroll
+                for (int q = 0; q < K; q++) s[q] += aa * ld_x(x + (int64_t)cc * ldx + q);
+            }
+        }
+        for (int o = C; o < 32; o <<= 1)
+#pragma unroll
+            for (int q = 0; q < K; q++) s[q] += __shfl_xor_sync(0xffffffffu, s[q], o);
+        if (lane < C) {
+#pragma unroll
+            for (int q = 0; q < K; q++) out[r * kMaxK + q] = s[q];
+        }
+    } else {
+        for (int r = lane; r < C; r += 32) {  // rows of the chunk, one lane each
+            V s[K];
+#pragma unroll
+            for (int q = 0; q < K; q++) s[q] = V(0);
+            for (int64_t k = pc.y; k < pc.z; k++) {
+                const int64_t idx = base + k * C + r;
+                const int cc = ld_stream(col + idx);
+                if (cc < 0) break;
+                const V aa = ld_stream(val + idx);
+#pragma unroll
+                for (int q = 0; q < K; q++) s[q] += aa * ld_x(x + (int64_t)cc * ldx + q);
+            }
+#pragma unroll
+            for (int q = 0; q < K; q++) out[r * kMaxK + q] = s[q];
+        }
+    }
+}
+
+// one thread per (long chunk, row): adds the chunk's pieces in order
+template <typename V, int K>
+__global__ void sliced_piece_fixup(int64_t nlong, int64_t m, int C, const int32_t *__restrict__ long_chunks,
+                                   const int32_t *__restrict__ piece_begin, const int32_t *__restrict__ reorder,
+                                   const V *__restrict__ partial, V alpha, V beta, V *__restrict__ y, int64_t ldy) {
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= nlong * C) return;
+    const int64_t L = tid / C;
+    const int r = (int)(tid - L * C);
+    const int64_t i = (int64_t)long_chunks[L] * C + r;
+    if (i >= m) return;
+    V s[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) s[q] = V(0);
+    for (int32_t p = piece_begin[L]; p < piece_begin[L + 1]; p++)
+#pragma unroll
+        for (int q = 0; q < K; q++) s[q] += partial[((int64_t)p * C + r) * kMaxK + q];
+    const int64_t row = reorder ? (int64_t)reorder[i] : i;
+    V *yp = y + row * ldy;
+#pragma unroll
+    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, s[q], beta, yp + q);
+}
+
 struct SlicedView {
     int64_t m;
     int32_t C;
@@ -93,15 +195,74 @@ struct SlicedView {
     const int32_t *reorder;
     const int32_t *col;
     const void *val;
+    int64_t nchunks;
 };
 
+// Piece plan of a sliced matrix, built on its first SpMV from the chunk
+// widths: extra[0] pieces (int4), extra[1] long chunk ids, extra[2] first
+// piece of each long chunk (+1 entry), extra[3] partial sums;
+// extra_i[0] pieces, extra_i[1] long chunks.
+sspmv_status ensure_piece_plan(const sspmv_features *f, const SlicedView &v, Plan *p, sspmv_stream_t s) {
+    if (p->extra_i[7]) return SSPMV_OK;
+    std::lock_guard<std::mutex> g(plan_mutex());
+    if (p->extra_i[7]) return SSPMV_OK;
+    std::vector<int64_t> cp((size_t)v.nchunks + 1);
+    SSPMV_CUDA_TRY(cudaMemcpyAsync(cp.data(), v.chunk_ptr, cp.size() * 8, cudaMemcpyDeviceToHost, cu(s)));
+    SSPMV_CUDA_TRY(cudaStreamSynchronize(cu(s)));
+    const int64_t piece_w = std::max<int64_t>(kLongWidth, kPieceElems / std::max<int32_t>(v.C, 1));
+    std::vector<int4> pieces;
+    std::vector<int32_t> longs, begin;
+    for (int64_t c = 0; c < v.nchunks; c++) {
+        const int64_t w = (cp[(size_t)c + 1] - cp[(size_t)c]) / v.C;
+        if (w <= kLongWidth) continue;
+        longs.push_back((int32_t)c);
+        begin.push_back((int32_t)pieces.size());
+        for (int64_t k0 = 0; k0 < w; k0 += piece_w)
+            pieces.push_back(make_int4((int)c, (int)k0, (int)std::min(w, k0 + piece_w), 0));
+    }
+    begin.push_back((int32_t)pieces.size());
+    if (!pieces.empty()) {
+        int4 *dp = nullptr;
+        int32_t *dl = nullptr, *db = nullptr;
+        unsigned char *part = nullptr;
+        SSPMV_TRY(dalloc(&dp, pieces.size(), s));
+        SSPMV_TRY(dalloc(&dl, longs.size(), s));
+        SSPMV_TRY(dalloc(&db, begin.size(), s));
+        SSPMV_TRY(dalloc(&part, pieces.size() * (size_t)v.C * kMaxK * vsize(f->value_type), s));
+        SSPMV_CUDA_TRY(cudaMemcpyAsync(dp, pieces.data(), pieces.size() * sizeof(int4), cudaMemcpyHostToDevice, cu(s)));
+        SSPMV_CUDA_TRY(cudaMemcpyAsync(dl, longs.data(), longs.size() * 4, cudaMemcpyHostToDevice, cu(s)));
+        SSPMV_CUDA_TRY(cudaMemcpyAsync(db, begin.data(), begin.size() * 4, cudaMemcpyHostToDevice, cu(s)));
+        SSPMV_CUDA_TRY(cudaStreamSynchronize(cu(s)));
+        p->extra[0] = dp;
+        p->extra[1] = dl;
+        p->extra[2] = db;
+        p->extra[3] = part;
+        p->extra_i[0] = (int64_t)pieces.size();
+        p->extra_i[1] = (int64_t)longs.size();
+    }
+    p->extra_i[7] = 1;
+    return SSPMV_OK;
+}
+
 template <typename V, int K>
-sspmv_status launch_sliced(const SlicedView &v, V alpha, const V *x, int64_t ldx, V beta, V *y, int64_t ldy,
-                           sspmv_stream_t s) {
+sspmv_status launch_sliced(const SlicedView &v, Plan *p, V alpha, const V *x, int64_t ldx, V beta, V *y,
+                           int64_t ldy, sspmv_stream_t s) {
+    const int64_t npieces = p ? p->extra_i[0] : 0;
     const unsigned grid = grid_for(v.m, kBlock, (int64_t)num_sms() * 16);
     sliced_spmv_kernel<V, K><<<grid, kBlock, 0, cu(s)>>>((int)v.m, v.C, v.chunk_ptr, v.reorder, v.col,
-                                                         (const V *)v.val, x, ldx, alpha, beta, y, ldy);
+                                                         (const V *)v.val, x, ldx, alpha, beta, y, ldy,
+                                                         npieces > 0 ? kLongWidth : INT64_MAX);
     SSPMV_LAUNCH_CHECK();
+    if (npieces > 0) {
+        const int64_t nlong = p->extra_i[1];
+        sliced_piece_kernel<V, K><<<grid_for(npieces * 32, kBlock), kBlock, 0, cu(s)>>>(
+            npieces, v.C, (const int4 *)p->extra[0], v.chunk_ptr, v.col, (const V *)v.val, x, ldx, (V *)p->extra[3]);
+        SSPMV_LAUNCH_CHECK();
+        sliced_piece_fixup<V, K><<<grid_for(nlong * v.C, 256), 256, 0, cu(s)>>>(
+            nlong, v.m, v.C, (const int32_t *)p->extra[1], (const int32_t *)p->extra[2], v.reorder,
+            (const V *)p->extra[3], alpha, beta, y, ldy);
+        SSPMV_LAUNCH_CHECK();
+    }
     return SSPMV_OK;
 }
 
@@ -109,15 +270,21 @@ sspmv_status spmm_sliced(const sspmv_features *f, const SlicedView &v, double al
                          int64_t ldx, double beta, void *Y, int64_t ldy, sspmv_stream_t s) {
     SSPMV_TRY(check_spmm_args(f, k, X, ldx, Y, ldy));
     if (v.m == 0) return SSPMV_OK;
+    Plan *p = nullptr;
+    if (v.nchunks > 0) {  // ELL (nchunks == 0 here) has no pieces
+        p = get_plan(f);
+        if (!p) return fail(SSPMV_OUT_OF_MEMORY, "plan allocation failed");
+        SSPMV_TRY(ensure_piece_plan(f, v, p, s));
+    }
     return dispatch_value(f->value_type, [&](auto tag) -> sspmv_status {
         using V = decltype(tag);
         return for_rhs_chunks<V>(k, (const V *)X, (V *)Y, [&](int32_t step, const V *xs, V *ys) {
             const V a = (V)alpha, b = (V)beta;
             switch (step) {
-            case 8: return launch_sliced<V, 8>(v, a, xs, ldx, b, ys, ldy, s);
-            case 4: return launch_sliced<V, 4>(v, a, xs, ldx, b, ys, ldy, s);
-            case 2: return launch_sliced<V, 2>(v, a, xs, ldx, b, ys, ldy, s);
-            default: return launch_sliced<V, 1>(v, a, xs, ldx, b, ys, ldy, s);
+            case 8: return launch_sliced<V, 8>(v, p, a, xs, ldx, b, ys, ldy, s);
+            case 4: return launch_sliced<V, 4>(v, p, a, xs, ldx, b, ys, ldy, s);
+            case 2: return launch_sliced<V, 2>(v, p, a, xs, ldx, b, ys, ldy, s);
+            default: return launch_sliced<V, 1>(v, p, a, xs, ldx, b, ys, ldy, s);
             }
         });
     });
@@ -340,7 +507,7 @@ extern "C" sspmv_status sspmv_spmm_ell(double alpha, const sspmv_ell *A, int32_t
     if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
     Plan *p = get_plan(&A->f);
     SlicedView v{A->f.num_rows, (int32_t)std::max<int64_t>(A->f.num_rows, 1), (const int64_t *)p->extra[0], nullptr,
-                 A->col_index, A->values};
+                 A->col_index, A->values, 0};
     return spmm_sliced(&A->f, v, alpha, k, X, ldx, beta, Y, ldy, s);
 }
 
@@ -414,7 +581,7 @@ extern "C" sspmv_status sspmv_csr_to_sell(const sspmv_csr *csr, int32_t C, int32
 extern "C" sspmv_status sspmv_spmm_sell(double alpha, const sspmv_s_ell *A, int32_t k, const void *X, int64_t ldx,
                                         double beta, void *Y, int64_t ldy, sspmv_stream_t s) {
     if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
-    SlicedView v{A->f.num_rows, A->sliceWidth, A->chunk_ptr, nullptr, A->col_index, A->values};
+    SlicedView v{A->f.num_rows, A->sliceWidth, A->chunk_ptr, nullptr, A->col_index, A->values, A->chunk_num};
     return spmm_sliced(&A->f, v, alpha, k, X, ldx, beta, Y, ldy, s);
 }
 
@@ -487,7 +654,7 @@ extern "C" sspmv_status sspmv_csr_to_sell_c_sigma(const sspmv_csr *csr, int32_t 
 extern "C" sspmv_status sspmv_spmm_sell_c_sigma(double alpha, const sspmv_sell_c_sigma *A, int32_t k, const void *X,
                                                 int64_t ldx, double beta, void *Y, int64_t ldy, sspmv_stream_t s) {
     if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
-    SlicedView v{A->f.num_rows, A->chunkWidth_C, A->chunk_ptr, A->reorder, A->col_index, A->values};
+    SlicedView v{A->f.num_rows, A->chunkWidth_C, A->chunk_ptr, A->reorder, A->col_index, A->values, A->validchunkNum};
     return spmm_sliced(&A->f, v, alpha, k, X, ldx, beta, Y, ldy, s);
 }
 
@@ -555,7 +722,7 @@ extern "C" sspmv_status sspmv_csr_to_sell_c_R(const sspmv_csr *csr, int32_t C, i
 extern "C" sspmv_status sspmv_spmm_sell_c_R(double alpha, const sspmv_sell_c_R *A, int32_t k, const void *X,
                                             int64_t ldx, double beta, void *Y, int64_t ldy, sspmv_stream_t s) {
     if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
-    SlicedView v{A->f.num_rows, A->chunkWidth_C, A->chunk_ptr, A->reorder, A->col_index, A->values};
+    SlicedView v{A->f.num_rows, A->chunkWidth_C, A->chunk_ptr, A->reorder, A->col_index, A->values, A->validchunkNum};
     return spmm_sliced(&A->f, v, alpha, k, X, ldx, beta, Y, ldy, s);
 }
 
