@@ -235,6 +235,22 @@ sspmv_status sspmv_LeSpMV_csr(double alpha, const sspmv_csr *A, const void *x, d
                               sspmv_stream_t stream);
 sspmv_status sspmv_spmm_csr(double alpha, const sspmv_csr *A, int32_t k, const void *X, int64_t ldx,
                             double beta, void *Y, int64_t ldy, sspmv_stream_t stream);
+/* Allocation-free CSR SpMV (no counterpart in the reference).  Same result as
+ * sspmv_LeSpMV_csr's merge-path kernel, for callers that cannot allocate
+ * device memory at SpMV time: a solver or serving loop whose device heap is
+ * owned by its own pool allocator, a latency-bound loop that cannot take
+ * cudaMalloc's implicit device synchronisation, a component held to a device
+ * memory budget enforced elsewhere.  Its scratch (tile split points and
+ * carries) lives in one fixed 16 MiB device array that every GPU loading this
+ * library keeps until exit; no per-matrix plan is built and nothing is
+ * allocated.  Limit: num_rows + num_nnzs <= 238,594,048 (116,501 tiles of
+ * 2048 merge items); larger matrices return SSPMV_INVALID_ARG.  The first call
+ * on a device looks up the array's address with that device current: make it
+ * before any stream capture.  All calls share the array: calls that overlap on
+ * the GPU race and must be serialised by the caller.  Nothing in the array
+ * needs clearing between calls (each call writes every entry it reads). */
+sspmv_status sspmv_LeSpMV_csr_noalloc(double alpha, const sspmv_csr *A, const void *x, double beta, void *y,
+                                      sspmv_stream_t stream);
 
 /* ---------------- ELL ---------------- */
 /* csr_to_ell (include/sparse_conversion.h:187-248) */

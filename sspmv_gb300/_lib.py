@@ -128,6 +128,7 @@ _SIGS = {
     "sspmv_delete_csr": (_st, [C.POINTER(Csr)]),
     "sspmv_LeSpMV_csr": (_st, [_d, C.POINTER(Csr), _vp, _d, _vp, _vp]),
     "sspmv_spmm_csr": (_st, [_d, C.POINTER(Csr), _i32, _vp, _i64, _d, _vp, _i64, _vp]),
+    "sspmv_LeSpMV_csr_noalloc": (_st, [_d, C.POINTER(Csr), _vp, _d, _vp, _vp]),
     "sspmv_algorithmic_bytes_csr": (_d, [C.POINTER(Csr), _i32, _i32]),
     "sspmv_read_mtx": (_st, [C.c_char_p, _i32, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64), _vp, _vp, _vp]),
     "sspmv_write_mtx": (_st, [C.c_char_p, _i64, _i64, _vp, _vp, _vp]),

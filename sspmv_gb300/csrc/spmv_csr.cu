@@ -428,3 +428,112 @@ extern "C" double sspmv_algorithmic_bytes_csr(const sspmv_csr *A, int32_t k, int
     return (double)A->f.num_nnzs * (sv + 4.0) + (double)(A->f.num_rows + 1) * 4.0 +
            (double)k * (double)A->f.num_cols * sv + (double)k * (double)A->f.num_rows * sv * (beta_nonzero ? 2.0 : 1.0);
 }
+
+// ===================================================== allocation-free CSR ===
+//
+// sspmv_LeSpMV_csr_noalloc: the merge-path CSR SpMV (one right-hand side)
+// with its scratch -- tile split points and per-tile carries -- in a fixed
+// device array that every GPU loading this library holds until the process
+// exits, so the call itself allocates nothing.
+//
+// Who needs it: code that cannot call cudaMalloc at SpMV time.  An iterative
+// solver or serving loop whose device heap is carved up by its own pool
+// allocator up front (a cudaMalloc there either fails or steals memory the
+// pool has promised elsewhere); a latency-bound loop where the implicit device
+// synchronisation of cudaMalloc/cudaFree is not acceptable; a component
+// running under a strict device-memory budget enforced outside this library.
+// The regular entry point builds a per-matrix plan on first use and keeps it
+// in device memory it allocates; this one does not.
+//
+// Limits and rules:
+//  - scratch is kNoAllocScratchBytes (16 MiB); a matrix needs
+//    ceil((num_rows + num_nnzs) / 2048) tiles of kNoAllocTileBytes each, so
+//    num_rows + num_nnzs may be at most kNoAllocMaxTiles * 2048 (about 238
+//    million); larger matrices get SSPMV_INVALID_ARG.
+//  - the first call on a device looks up the array's device address
+//    (cudaGetSymbolAddress) with that device current; make that first call
+//    before any stream capture.
+//  - every call writes all the scratch it later reads (split points, carries),
+//    so nothing has to be cleared between calls; but all calls share the one
+//    array: calls that overlap on the GPU (different streams, or a graph
+//    replayed concurrently) race on it and must be serialised by the caller.
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 16u << 20;
+constexpr int kNoAllocTile = MergeShape<1>::tile;  // 2048 merge items
+// per tile: split point (int2) + carry_row + has_end + carry and head values
+// (kMaxK slots of up to 8 bytes each, the layout csr_merge_kernel uses)
+constexpr size_t kNoAllocTileBytes = sizeof(int2) + 4 + 4 + 2 * kMaxK * 8;
+constexpr int64_t kNoAllocMaxTiles = (int64_t)((kNoAllocScratchBytes - 4 * 256 - sizeof(int2)) / kNoAllocTileBytes);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void *g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
+
+sspmv_status noalloc_scratch(void **out) {
+    int dev = 0;
+    SSPMV_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(SSPMV_NOT_SUPPORTED, "device ordinal %d too large", dev);
+    std::lock_guard<std::mutex> g(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(SSPMV_CUDA_ERROR, "cudaGetSymbolAddress(scratch) on device %d: %s", dev, cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return SSPMV_OK;
+}
+
+inline size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+}  // namespace
+
+extern "C" sspmv_status sspmv_LeSpMV_csr_noalloc(double alpha, const sspmv_csr *A, const void *x, double beta,
+                                                 void *y, sspmv_stream_t s) {
+    if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
+    SSPMV_TRY(check_spmm_args(&A->f, 1, x, 1, y, 1));
+    const int64_t m = A->f.num_rows, nnz = A->f.num_nnzs;
+    if (m == 0) return SSPMV_OK;
+    const int64_t tiles = std::max<int64_t>((m + nnz + kNoAllocTile - 1) / kNoAllocTile, 1);
+    if (tiles > kNoAllocMaxTiles)
+        return fail(SSPMV_INVALID_ARG,
+                    "sspmv_LeSpMV_csr_noalloc: num_rows + num_nnzs = %lld exceeds the fixed scratch limit of %lld "
+                    "(%lld tiles of %d); use sspmv_LeSpMV_csr",
+                    (long long)(m + nnz), (long long)(kNoAllocMaxTiles * kNoAllocTile), (long long)kNoAllocMaxTiles,
+                    kNoAllocTile);
+    void *base = nullptr;
+    SSPMV_TRY(noalloc_scratch(&base));
+    unsigned char *b = (unsigned char *)base;
+    size_t off = 0;
+    int2 *coords = (int2 *)(b + off);
+    off = align256(off + (size_t)(tiles + 1) * sizeof(int2));
+    int32_t *carry_row = (int32_t *)(b + off);
+    off = align256(off + (size_t)tiles * 4);
+    int32_t *has_end = (int32_t *)(b + off);
+    off = align256(off + (size_t)tiles * 4);
+    unsigned char *carry_val = b + off;
+    off = align256(off + (size_t)tiles * kMaxK * 8);
+    unsigned char *head_val = b + off;
+    merge_path_search<<<grid_for(tiles + 1, 256), 256, 0, cu(s)>>>(tiles, kNoAllocTile, (int)m, (int)nnz,
+                                                                    A->row_offset, coords);
+    SSPMV_LAUNCH_CHECK();
+    return dispatch_value(A->f.value_type, [&](auto tag) -> sspmv_status {
+        using V = decltype(tag);
+        const size_t smem = (size_t)kNoAllocTile * sizeof(V) + ((size_t)kNoAllocTile + 1) * 4;
+        csr_merge_kernel<V, 1><<<(unsigned)tiles, kBlock, smem, cu(s)>>>(
+            (int)m, A->row_offset, A->col_index, (const V *)A->values, (const V *)x, 1, (V)alpha, (V)beta, (V *)y, 1,
+            coords, carry_row, has_end, (V *)carry_val, (V *)head_val);
+        SSPMV_LAUNCH_CHECK();
+        if (tiles > 1) {
+            csr_merge_fixup<V, 1><<<grid_for(tiles, 256), 256, 0, cu(s)>>>(
+                tiles, (int)m, A->row_offset, coords, carry_row, has_end, (const V *)carry_val, (const V *)head_val,
+                (V)alpha, (V)beta, (V *)y, 1);
+            SSPMV_LAUNCH_CHECK();
+        }
+        return SSPMV_OK;
+    });
+}
