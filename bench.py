@@ -51,6 +51,7 @@ def parse_args():
     ap.add_argument("--scale", type=float, default=1.0, help="row-count scale (testing only)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (library defaults)")
+    ap.add_argument("--csr-kernel", default="", help="pin the CSR kernel as FLAG:PARAM (implies no tuning of CSR)")
     return ap.parse_args()
 
 
@@ -177,11 +178,16 @@ def run_gpu(args, rank, world):
                               "rows": A.num_rows, "cols": A.num_cols})
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
+    if args.csr_kernel:
+        flag, param = (int(v) for v in args.csr_kernel.split(":"))
+        for c in cases:
+            if c["fmt"] == "csr":
+                c["M"].set_kernel(flag, param)
     if not args.no_tune:
         from sspmv_gb300 import autotune
         seen = set()
         for c in cases:
-            if id(c["M"]) in seen:  # CSR is shared by a family's formats
+            if id(c["M"]) in seen or (args.csr_kernel and c["fmt"] == "csr"):
                 continue
             seen.add(id(c["M"]))
             res = autotune.tune_format(c["M"], c["x"], c["y"])

@@ -392,6 +392,20 @@ double sspmv_algorithmic_bytes_sell(const sspmv_s_ell *A, int32_t k, int32_t bet
 double sspmv_algorithmic_bytes_sell_c_sigma(const sspmv_sell_c_sigma *A, int32_t k, int32_t beta_nonzero);
 double sspmv_algorithmic_bytes_sell_c_R(const sspmv_sell_c_R *A, int32_t k, int32_t beta_nonzero);
 
+/* ---------------- matrix features ---------------- */
+/* The reference's MTX feature extractor (src/sparse_features.cpp:122-968) on
+ * a device CSR matrix: features[0..39] are the 40 values of its .features
+ * file in file order (FeaturesWrite, :1347-1400), features[40..61] the other
+ * statistics it computes (triangle and diagonal counts, minima, dominance,
+ * value ranges, symmetry, variances, GrX = -1 as the reference leaves them).
+ * tile_blocks: T for the T x T tile grid (0 = 256, the shipped
+ * MAT_TILE_SIZE).  nnz_by_tiles / uniq_rb / uniq_cb: optional host arrays of
+ * T*T counts (nonzeros, distinct rows, distinct columns per tile). */
+#define SSPMV_NUM_FEATURES 62
+sspmv_status sspmv_csr_features(const sspmv_csr *A, int32_t tile_blocks, double *features, int32_t *nnz_by_tiles,
+                                int32_t *uniq_rb, int32_t *uniq_cb, sspmv_stream_t stream);
+const char *sspmv_feature_name(int32_t i);
+
 /* ---------------- host utilities ---------------- */
 /* Matrix Market reader (utils/sparse_io.cpp:27-204: coordinate format,
  * general/symmetric, real/integer/pattern; symmetric entries mirrored,

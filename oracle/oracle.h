@@ -185,6 +185,13 @@ ORACLE_DECLARE(float, f32)
 
 int oracle_max_threads(void);
 
+/* Matrix features (class MTX, src/sparse_features.cpp:122-968) of a general
+ * CSR matrix with T x T tiles: F receives the 62 values in the library's
+ * feature order; nnz_by_tiles / uniq_rb / uniq_cb (T*T each, may be NULL)
+ * receive the per-tile counts. */
+void oracle_features(int32_t m, int32_t n, const int32_t *rowptr, const int32_t *col, const double *val,
+                     int32_t T, double *F, int32_t *nnz_by_tiles, int32_t *uniq_rb, int32_t *uniq_cb);
+
 #ifdef __cplusplus
 }
 #endif

@@ -241,6 +241,17 @@ class Oracle:
             float(alpha), float(beta), _ptr(Y0c), k, _ptr(y), _ptr(ab), nthreads)
         return (y.reshape(m), ab.reshape(m)) if X.ndim == 1 else (y, ab)
 
+    def features(self, csr, T=256):
+        """MTX features (62, library order) and per-tile counts of a CSR."""
+        L = self.lib
+        L.oracle_features.argtypes = [_i32, _i32, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp]
+        F = np.zeros(62)
+        t, u, v = (np.zeros(T * T, np.int32) for _ in range(3))
+        val = np.ascontiguousarray(csr.values, np.float64)
+        L.oracle_features(csr.num_rows, csr.num_cols, _ptr(csr.row_offset), _ptr(csr.col_index), _ptr(val), T,
+                          _ptr(F), _ptr(t), _ptr(u), _ptr(v))
+        return F, {"tiles": t, "urb": u, "ucb": v}
+
     def max_rel_error(self, a, b):
         return float(getattr(self.lib, f"oracle_max_rel_error_{_sfx(a.dtype)}")(
             _ptr(a), _ptr(b), _i64(a.size)))

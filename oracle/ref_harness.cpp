@@ -12,10 +12,18 @@
  * flattened chunk by chunk (each chunk row-major as the reference stores it).
  * Free every returned array with ref_free().
  */
-#include "LeSpMV.h"
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+#include <iostream>
+// The feature extractor keeps its results in private members of class MTX;
+// the harness reads them directly (same class layout, access opened).
+#define private public
+#include "LeSpMV.h"
+#undef private
 
 extern "C" {
 
@@ -248,7 +256,49 @@ static int do_read(const char *path, ref_out *o) {
     return 0;
 }
 
-#define REF_EXPORT(V, S)                                                                        \
+/* MTX feature extraction of a Matrix Market file (MtxLoad + CalculateFeatures
+ * + CalculateTilesExtraFeatures, src/sparse_features.cpp), in the library's
+ * feature order (62 values); arrays: nnz_by_Tiles_, uniq_RB, uniq_CB. */
+template <typename V>
+static int do_features(const char *path, double *F, ref_out *o) {
+    MTX<int, V> x;
+    if (!x.MtxLoad(path)) return -1;
+    x.CalculateFeatures();
+    x.CalculateTilesExtraFeatures(path);
+    double v[62] = {
+        (double)x.num_rows, (double)x.num_cols, (double)x.num_nnzs, (double)x.nnz_ratio_,
+        (double)x.diag_close_ratio_, (double)x.distance_per_row_ / x.num_cols, (double)x.nz_row_ratio_,
+        (double)x.max_nnz_each_row_, (double)x.ave_nnz_each_row_, (double)x.standard_dev_row_,
+        (double)x.P_ratio_row_, (double)x.Gini_row_, (double)x.nz_col_ratio_, (double)x.max_nnz_each_col_,
+        (double)x.ave_nnz_each_col_, (double)x.standard_dev_col_, (double)x.P_ratio_col_, (double)x.Gini_col_,
+        (double)x.t_nz_ratio_tiles_, (double)x.t_max_nnz_all_tiles_, (double)x.t_ave_nnz_all_tiles,
+        (double)x.t_standard_dev_all_tiles, (double)x.t_P_ratio_all_tiles_, (double)x.t_Gini_all_tiles_,
+        (double)x.t_nz_ratio_RB_, (double)x.t_max_nnz_each_RB_, (double)x.t_ave_nnz_RB, (double)x.t_standard_dev_RB,
+        (double)x.t_P_ratio_RB_, (double)x.t_Gini_RB_, (double)x.t_nz_ratio_CB_, (double)x.t_max_nnz_each_CB_,
+        (double)x.t_ave_nnz_CB, (double)x.t_standard_dev_CB, (double)x.t_P_ratio_CB_, (double)x.t_Gini_CB_,
+        (double)x.uniqR, (double)x.uniqC, (double)x.potReuseR, (double)x.potReuseC,
+        (double)x.nnz_lower_, (double)x.nnz_upper_, (double)x.nnz_diagonal_, (double)x.complete_ndiags,
+        (double)x.min_nnz_each_row_, (double)x.min_nnz_each_col_, (double)x.diagonal_dominant_ratio_,
+        (double)x.max_value_offdiag_, (double)x.max_value_diagonal_, (double)x.row_variability_,
+        (double)x.col_variability_, (double)x.pattern_symm_, (double)x.value_symm_,
+        (double)x.t_min_nnz_all_tiles_, (double)x.t_min_nnz_each_RB_, (double)x.t_min_nnz_each_CB_,
+        (double)x.var_nnz_each_row_, (double)x.var_nnz_each_col_, (double)x.GrX_uniqR, (double)x.GrX_uniqC,
+        (double)x.GrX_potReuseR, (double)x.GrX_potReuseC};
+    memcpy(F, v, sizeof(v));
+    o->ints[0] = x.t_num_blocks;
+    o->arrays[0] = dup(x.nnz_by_Tiles_.data(), (int64_t)x.nnz_by_Tiles_.size());
+    o->lens[0] = (int64_t)x.nnz_by_Tiles_.size();
+    o->arrays[1] = dup(x.uniq_RB.data(), (int64_t)x.uniq_RB.size());
+    o->lens[1] = (int64_t)x.uniq_RB.size();
+    o->arrays[2] = dup(x.uniq_CB.data(), (int64_t)x.uniq_CB.size());
+    o->lens[2] = (int64_t)x.uniq_CB.size();
+    return 0;
+}
+
+extern "C" int ref_features_f64(const char *path, double *F, ref_out *o) { return do_features<double>(path, F, o); }
+extern "C" int ref_features_f32(const char *path, double *F, ref_out *o) { return do_features<float>(path, F, o); }
+
+#define REF_EXPORT(V, S)                                                                      \
     extern "C" void ref_coo_to_csr_##S(int m, int n, int nnz, const int *ri, const int *ci,       \
                                        const V *v, ref_out *o) { do_coo_to_csr<V>(m, n, nnz, ri, ci, v, o); } \
     extern "C" void ref_csr_to_ell_##S(int m, int n, const int *rp, const int *ci, const V *v,    \

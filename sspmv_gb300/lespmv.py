@@ -300,6 +300,26 @@ def csr_from_host(A: HostCSR, stream=None) -> CSR_Matrix:
     return CSR_Matrix(s)
 
 
+FEATURE_NAMES = [lib.sspmv_feature_name(i).decode() for i in range(_lib.NUM_FEATURES)]
+
+
+def features(csr: CSR_Matrix, tile_blocks: int = 256, arrays: bool = False, stream=None):
+    """MTX feature extraction on the GPU (src/sparse_features.cpp): a vector of
+    62 features (names in FEATURE_NAMES), and with arrays=True the per-tile
+    nonzero / distinct-row / distinct-column counts (T*T each)."""
+    F = np.zeros(_lib.NUM_FEATURES)
+    TT = tile_blocks * tile_blocks
+    t = np.zeros(TT, np.int32) if arrays else None
+    u = np.zeros(TT, np.int32) if arrays else None
+    v = np.zeros(TT, np.int32) if arrays else None
+    ptr = (lambda a: a.ctypes.data_as(C.c_void_p) if a is not None else None)
+    call("sspmv_csr_features", csr.ref(), int(tile_blocks), F.ctypes.data_as(C.c_void_p), ptr(t), ptr(u), ptr(v),
+         _stream(stream))
+    if arrays:
+        return F, {"tiles": t, "urb": u, "ucb": v}
+    return F
+
+
 def read_csr_matrix(path: str, precision: int = 64) -> HostCSR:
     """read_csr_matrix (utils/sparse_io.cpp:180-204) on the host."""
     vt = F64 if precision == 64 else F32

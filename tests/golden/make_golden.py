@@ -144,11 +144,35 @@ def main() -> None:
                 rec["spmv"].append([fmt, flag])
             if name == "dups":
                 rec["coo_to_csr"] = {k: digest(v) for k, v in coo_out.items()}
+            if A.nnz > 0:
+                F, arrs = ref_features(ref, A)
+                arrays["features"] = F
+                rec["feature_arrays"] = {k: digest(v) for k, v in arrs.items()}
             fname = f"{name}_{tag}.npz"
             np.savez_compressed(OUT / fname, **arrays, meta=np.frombuffer(json.dumps(rec).encode(), np.uint8))
             index[fname] = {"num_rows": A.num_rows, "nnz": A.nnz}
             print(fname, A.num_rows, A.nnz)
     (OUT / "INDEX.json").write_text(json.dumps(index, indent=1, sort_keys=True) + "\n")
+
+
+def ref_features(ref: Reference, A):
+    """The reference's MTX features (double build, T = 256) of A written as a
+    Matrix Market file (row-major order = CSR order), in the library's
+    feature order, plus its per-tile nonzero / distinct-row / distinct-column
+    counts."""
+    import ctypes as C
+    import tempfile
+    from oracle import RefOut
+    from sspmv_gb300.lespmv import write_mtx
+    with tempfile.TemporaryDirectory() as d:
+        path = Path(d) / "m.mtx"
+        write_mtx(str(path), A)
+        F = np.zeros(62)
+        o = RefOut()
+        rc = ref.lib.ref_features_f64(str(path).encode(), C.c_void_p(F.ctypes.data), C.byref(o))
+        assert rc == 0
+        arrs = ref._take(o, [("tiles", np.int32), ("urb", np.int32), ("ucb", np.int32)])
+    return F, arrs
 
 
 def ref_dia_too_wide(ref, A) -> bool:
