@@ -190,6 +190,16 @@ def run_gpu(args, rank, world):
             if id(c["M"]) in seen or (args.csr_kernel and c["fmt"] == "csr"):
                 continue
             seen.add(id(c["M"]))
+            if c["fmt"] in ("sell", "sell_c_sigma", "sell_c_R", "csr5", "bsr"):
+                M2, rec = autotune.tune_conversion(c["csr"], c["fmt"], c["x"], c["y"])
+                if M2 is not None:
+                    if c["M"] is not c["csr"]:
+                        c["M"].delete()
+                    c["M"] = M2
+                    c["bytes"] = M2.algorithmic_bytes(1, False)
+                    c["tuned"] = {"params": rec["params"], "ms": rec["ms"]}
+                log(f"tuned {c['fam']}/{c['fmt']}/{c['dt']}: {c.get('tuned')}")
+                continue
             res = autotune.tune_format(c["M"], c["x"], c["y"])
             c["tuned"] = res["best"] if res else None
     for c in cases:

@@ -61,7 +61,57 @@ def tune_csr(M, x, y, reps: int = 10) -> dict:
 
 
 # Kernel candidates per format (formats with one kernel are not listed).
-KERNEL_CANDIDATES = {"csr": CSR_CANDIDATES}
+KERNEL_CANDIDATES = {"csr": CSR_CANDIDATES, "coo": [(0, 0), (1, 0)]}
+
+
+def conversion_candidates(fmt: str, num_rows: int) -> list[dict]:
+    """Converter parameters tried per format (the reference's defaults first)."""
+    if fmt == "sell":
+        return [dict(chunkwidth=c, alignment=a) for c in (4, 8, 16, 32) for a in (0, 1)]
+    if fmt == "sell_c_sigma":
+        sig_n = max(32, -(-num_rows // 32) * 32)  # sigma = N, a multiple of every C tried
+        out = [dict(slicewidth=0, chunkwidth=0, alignment=0)]
+        out += [dict(slicewidth=s, chunkwidth=c, alignment=a) for c in (8, 16, 32) for s in (256, 4096, sig_n)
+                for a in (0, 1)]
+        return out
+    if fmt == "sell_c_R":
+        return [dict(chunkwidth=c, alignment=a) for c in (4, 8, 16, 32) for a in (0, 1)]
+    if fmt == "csr5":
+        return [dict(sigma=0, omega=0), dict(sigma=16, omega=32), dict(sigma=32, omega=32), dict(sigma=8, omega=32),
+                dict(sigma=16, omega=16)]
+    if fmt == "bsr":
+        return [dict(blockDimRow=r, blockDimCol=c) for r, c in ((2, 2), (4, 4), (8, 8), (2, 4), (4, 2), (4, 8),
+                                                                (8, 4), (1, 4), (4, 1))]
+    return []
+
+
+def tune_conversion(csr, fmt: str, x, y, reps: int = 8, max_fill: float = 4.0):
+    """Converts `csr` with each candidate parameter set of `fmt`, times one
+    SpMV of each and keeps the fastest.  Returns (matrix, record) or
+    (None, None) when no candidate converts."""
+    import torch
+    flush = torch.empty(L2_FLUSH // 4, dtype=torch.float32, device=x.device)
+    best, table = None, []
+    for kw in conversion_candidates(fmt, csr.num_rows):
+        if fmt == "bsr":
+            nnzb = L.count_blocks(csr, kw["blockDimRow"], kw["blockDimCol"])
+            if nnzb * kw["blockDimRow"] * kw["blockDimCol"] > max_fill * max(csr.num_nnzs, 1):
+                continue
+        try:
+            M = getattr(L, f"csr_to_{fmt}")(csr, **kw)
+        except L.SSPMVError:
+            continue
+        ms = time_spmv(M, x, y, reps, flush=flush)
+        table.append({"params": kw, "ms": ms})
+        if best is None or ms < best[1]:
+            if best is not None:
+                best[0].delete()
+            best = (M, ms, kw)
+        else:
+            M.delete()
+    if best is None:
+        return None, None
+    return best[0], {"format": fmt, "params": best[2], "ms": best[1], "table": table}
 
 
 def tune_format(M, x, y, reps: int = 10) -> dict | None:

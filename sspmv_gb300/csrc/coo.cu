@@ -6,13 +6,15 @@
 //
 // SpMV (LeSpMV_coo, src/spmv_coo.cpp:161-182).  The reference scales y by
 // beta, then scatters alpha*a*x with OpenMP atomics (and skips the scaling
-// when beta == 0, leaving stale y).  Here, for row-sorted COO, CTAs take
-// equal tiles of nonzeros, stage products and row ids in shared memory and
-// reduce runs of equal rows with a block-wide segmented scan; rows that cross
-// tile boundaries are finished by a second kernel in a fixed order, and rows
-// with no nonzeros (listed once, when the plan is built) get y = beta*y.  No
-// atomics: results are deterministic.  Unsorted COO (row_sorted == 0) uses a
-// scale pass plus an atomic scatter, like the reference.
+// when beta == 0, leaving stale y).  Here, for row-sorted COO, each warp takes
+// 256 consecutive nonzeros and reduces runs of equal rows with a segmented
+// shuffle scan (kernel_flag 0, default); kernel_flag 1 uses CTA tiles of 2048
+// nonzeros staged in shared memory with a block-wide segmented scan.  Rows
+// that cross chunk boundaries are finished by a second kernel in a fixed
+// order, and rows with no nonzeros (listed once, when the plan is built) get
+// y = beta*y.  No atomics: results are deterministic.  Unsorted COO
+// (row_sorted == 0) uses a scale pass plus an atomic scatter, like the
+// reference.
 #include <algorithm>
 
 #include "common.cuh"
@@ -265,6 +267,94 @@ __global__ void __launch_bounds__(kBlock) coo_tile_kernel(
     }
 }
 
+// Warp kernel (default): a warp takes kWarpChunk consecutive nonzeros in
+// steps of 32, runs a segmented shuffle scan keyed by row over each step and
+// carries the open row into the next step.  A lane whose nonzero is the last
+// of its row writes that row -- unless the row began before the warp's chunk
+// (head piece) -- and the chunk's open last row is left as a carry.  No
+// shared memory, no barriers.
+constexpr int kWarpChunk = 256;
+
+template <typename V, int K>
+__global__ void __launch_bounds__(kBlock) coo_warp_kernel(
+    int64_t nnz, const int32_t *__restrict__ ri, const int32_t *__restrict__ ci, const V *__restrict__ cv,
+    const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
+    int32_t *__restrict__ carry_row, int32_t *__restrict__ has_end, V *__restrict__ carry_val,
+    V *__restrict__ head_val) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t j0 = w * kWarpChunk;
+    if (j0 >= nnz) return;
+    const int64_t j1 = min(j0 + (int64_t)kWarpChunk, nnz);
+    const int first_row = __ldg(ri + j0);
+    const bool head_open = j0 > 0 && __ldg(ri + j0 - 1) == first_row;  // chunk starts inside a row
+    int carry_r = -1;
+    V carry[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) carry[q] = V(0);
+    bool first_ended = false;
+    for (int64_t base = j0; base < j1; base += 32) {
+        const int64_t e = base + lane;
+        const bool valid = e < j1;
+        int r = -1 - lane;  // unique keys for idle lanes
+        V p[K];
+#pragma unroll
+        for (int q = 0; q < K; q++) p[q] = V(0);
+        if (valid) {
+            r = ld_stream(ri + e);
+            const int c = ld_stream(ci + e);
+            const V a = ld_stream(cv + e);
+#pragma unroll
+            for (int q = 0; q < K; q++) p[q] = a * ld_x(x + (int64_t)c * ldx + q);
+        }
+        if (lane == 0 && r == carry_r) {
+#pragma unroll
+            for (int q = 0; q < K; q++) p[q] += carry[q];
+        }
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int r2 = __shfl_up_sync(0xffffffffu, r, o);
+            V v2[K];
+#pragma unroll
+            for (int q = 0; q < K; q++) v2[q] = __shfl_up_sync(0xffffffffu, p[q], o);
+            if (lane >= o && r2 == r) {
+#pragma unroll
+                for (int q = 0; q < K; q++) p[q] += v2[q];
+            }
+        }
+        // row of the next nonzero in the matrix
+        int rn = __shfl_down_sync(0xffffffffu, r, 1);
+        if (valid && (lane == 31 || e + 1 >= j1)) rn = e + 1 < nnz ? __ldg(ri + e + 1) : -1;
+        const bool ends = valid && rn != r;
+        if (ends) {
+            if (r == first_row && head_open) {
+                V *hp = head_val + w * kMaxK;
+#pragma unroll
+                for (int q = 0; q < K; q++) hp[q] = p[q];
+            } else {
+                V *yp = y + (int64_t)r * ldy;
+#pragma unroll
+                for (int q = 0; q < K; q++) yp[q] = axpby(alpha, p[q], beta, yp + q);
+            }
+        }
+        if (__any_sync(0xffffffffu, ends && r == first_row)) first_ended = true;
+        // open row at the end of this step -> next step / next chunk
+        const int last = (int)min((int64_t)31, j1 - 1 - base);
+        carry_r = __shfl_sync(0xffffffffu, ends ? -2 : r, last);
+#pragma unroll
+        for (int q = 0; q < K; q++) carry[q] = __shfl_sync(0xffffffffu, p[q], last);
+    }
+    if (lane == 0) {
+        has_end[w] = first_ended ? 1 : 0;
+        carry_row[w] = carry_r >= 0 ? carry_r : -1;
+        if (carry_r >= 0) {
+            V *cp = carry_val + w * kMaxK;
+#pragma unroll
+            for (int q = 0; q < K; q++) cp[q] = carry[q];
+        }
+    }
+}
+
 template <typename V, int K>
 __global__ void coo_fixup(int64_t ntiles, const int32_t *__restrict__ ri, int tile,
                           const int32_t *__restrict__ carry_row, const int32_t *__restrict__ has_end,
@@ -304,7 +394,7 @@ struct CooPlan {
     void *head_val[2] = {nullptr, nullptr};
 };
 
-// extra[0..]: carry buffers per tile size, extra[6] = absent-row list
+// extra[0..]: carry buffers per tile size, extra[10] = absent-row list (extra[6..8]: warp chunks)
 sspmv_status ensure_coo_plan(const sspmv_coo *A, Plan *p, int which, int tile, sspmv_stream_t s) {
     if (p->extra[which * 3]) return SSPMV_OK;
     std::lock_guard<std::mutex> g(plan_mutex());
@@ -317,7 +407,7 @@ sspmv_status ensure_coo_plan(const sspmv_coo *A, Plan *p, int which, int tile, s
     SSPMV_TRY(dalloc(&ints, (size_t)nt * 2, s));
     SSPMV_TRY(dalloc(&cv, (size_t)nt * kMaxK * sv, s));
     SSPMV_TRY(dalloc(&hv, (size_t)nt * kMaxK * sv, s));
-    if (!p->extra[6]) {  // rows without nonzeros
+    if (!p->extra[10]) {  // rows without nonzeros
         int32_t *flag = nullptr, *pos = nullptr, *list = nullptr;
         int32_t cnt = 0;
         SSPMV_TRY(dalloc(&flag, (size_t)m, s));
@@ -339,8 +429,8 @@ sspmv_status ensure_coo_plan(const sspmv_coo *A, Plan *p, int which, int tile, s
         }
         dfree(flag, s);
         dfree(pos, s);
-        p->extra[6] = list;
-        p->extra_i[6] = cnt;
+        p->extra[10] = list;
+        p->extra_i[10] = cnt;
     }
     p->extra_i[which * 3] = nt;
     p->extra[which * 3 + 1] = cv;
@@ -363,18 +453,33 @@ sspmv_status coo_pass(const sspmv_coo *A, Plan *p, V alpha, const V *x, int64_t 
         }
         return SSPMV_OK;
     }
-    constexpr int tile = CooShape<K>::tile;
-    const int which = K <= 4 ? 0 : 1;
+    const bool warp_kernel = A->f.kernel_flag != 1;
+    const int tile = warp_kernel ? kWarpChunk : CooShape<K>::tile;
+    const int which = warp_kernel ? 2 : (K <= 4 ? 0 : 1);
     SSPMV_TRY(ensure_coo_plan(A, p, which, tile, s));
     const int64_t nt = p->extra_i[which * 3];
     int32_t *ints = (int32_t *)p->extra[which * 3];
-    const int64_t nabs = p->extra_i[6];
+    const int64_t nabs = p->extra_i[10];
     if (nabs > 0) {
         scale_rows<V, K><<<grid_for(nabs, 256, (int64_t)num_sms() * 16), 256, 0, cu(s)>>>(
-            nabs, (const int32_t *)p->extra[6], beta, y, ldy);
+            nabs, (const int32_t *)p->extra[10], beta, y, ldy);
         SSPMV_LAUNCH_CHECK();
     }
     if (nnz == 0) return SSPMV_OK;
+    if (warp_kernel) {
+        coo_warp_kernel<V, K><<<grid_for(nt * 32, kBlock), kBlock, 0, cu(s)>>>(
+            nnz, A->row_index, A->col_index, (const V *)A->values, x, ldx, alpha, beta, y, ldy, ints, ints + nt,
+            (V *)p->extra[which * 3 + 1], (V *)p->extra[which * 3 + 2]);
+        SSPMV_LAUNCH_CHECK();
+        if (nt > 1) {
+            coo_fixup<V, K><<<grid_for(nt, 256), 256, 0, cu(s)>>>(nt, A->row_index, tile, ints, ints + nt,
+                                                                  (const V *)p->extra[which * 3 + 1],
+                                                                  (const V *)p->extra[which * 3 + 2], alpha, beta, y,
+                                                                  ldy);
+            SSPMV_LAUNCH_CHECK();
+        }
+        return SSPMV_OK;
+    }
     const size_t smem = (size_t)tile * K * sizeof(V) + (size_t)tile * 4;
     static bool attr = false;
     if (!attr) {

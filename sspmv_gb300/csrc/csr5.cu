@@ -364,9 +364,28 @@ __global__ void __launch_bounds__(kBlock) csr5_tile_kernel(C5View A, const V *__
     }
 }
 
+__global__ void count_empty_rows(int64_t rows, const int32_t *__restrict__ rp, unsigned long long *out) {
+    unsigned long long c = 0;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x)
+        c += rp[r] == rp[r + 1];
+    c = warp_sum(c);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+// y = beta*y on the empty rows before the tail tile (thread per row).
+template <typename V, int K>
+__global__ void __launch_bounds__(kBlock) csr5_empty_rows(int64_t rows, const int32_t *__restrict__ rp, V beta,
+                                                        V *__restrict__ y, int64_t ldy) {
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x)
+        if (ld_stream(rp + r) == ld_stream(rp + r + 1)) {
+            V *yp = y + r * ldy;
+#pragma unroll
+            for (int q = 0; q < K; q++) yp[q] = beta == V(0) ? V(0) : beta * yp[q];
+        }
+}
+
 // Rows from the tail tile on (CSR dot products, warp per row; the first one is
-// clipped to the tail when it began earlier) and y = beta*y on the empty rows
-// before it.
+// clipped to the tail when it began earlier).
 template <typename V, int K>
 __global__ void __launch_bounds__(kBlock) csr5_rows_kernel(C5View A, int32_t tail_row, int64_t tail_start,
                                                          const V *__restrict__ x, int64_t ldx, V alpha, V beta,
@@ -374,17 +393,9 @@ __global__ void __launch_bounds__(kBlock) csr5_rows_kernel(C5View A, int32_t tai
                                                          V *__restrict__ head_val) {
     const int lane = threadIdx.x & 31;
     const V *val = (const V *)A.val;
-    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < A.m;
+    for (int64_t r = tail_row + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); r < A.m;
          r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
         const int32_t rs = A.rp[r], re = A.rp[r + 1];
-        if (r < tail_row) {
-            if (rs == re && lane == 0) {
-                V *yp = y + r * ldy;
-#pragma unroll
-                for (int q = 0; q < K; q++) yp[q] = beta == V(0) ? V(0) : beta * yp[q];
-            }
-            continue;
-        }
         const bool clipped = r == tail_row && rs < tail_start;
         const int64_t s0 = clipped ? tail_start : rs;
         V s[K];
@@ -473,6 +484,20 @@ sspmv_status ensure_c5_plan(const sspmv_csr5 *A, Plan *pl, sspmv_stream_t s) {
     SSPMV_TRY(dalloc(&cv, (size_t)p * kMaxK * sv, s));
     SSPMV_TRY(dalloc(&hv, (size_t)p * kMaxK * sv, s));
     SSPMV_CUDA_TRY(cudaMemsetAsync(ints, 0, (size_t)p * 8, cu(s)));
+    // empty rows before the tail tile (they get y = beta*y in a separate pass)
+    const int64_t tail_row = A->_p > 0 ? A->tail_partition_start : 0;
+    unsigned long long *cnt = nullptr, h = 0;
+    SSPMV_TRY(dalloc(&cnt, 1, s));
+    SSPMV_CUDA_TRY(cudaMemsetAsync(cnt, 0, 8, cu(s)));
+    if (tail_row > 0) {
+        count_empty_rows<<<grid_for(tail_row, 256, (int64_t)num_sms() * 16), 256, 0, cu(s)>>>(tail_row, A->row_offset,
+                                                                                             cnt);
+        note_launch();
+    }
+    SSPMV_CUDA_TRY(cudaMemcpyAsync(&h, cnt, 8, cudaMemcpyDeviceToHost, cu(s)));
+    SSPMV_CUDA_TRY(cudaStreamSynchronize(cu(s)));
+    dfree(cnt, s);
+    pl->extra_i[3] = (int64_t)h;
     pl->extra[1] = cv;
     pl->extra[2] = hv;
     pl->extra[0] = ints;
@@ -509,8 +534,13 @@ sspmv_status csr5_pass(const sspmv_csr5 *A, Plan *pl, V alpha, const V *x, int64
     }
     const int64_t tail_start = A->_p > 0 ? (int64_t)(A->_p - 1) * A->sigma * A->omega : 0;
     const int32_t tail_row = A->_p > 0 ? A->tail_partition_start : 0;
-    csr5_rows_kernel<V, K><<<grid_for(A->f.num_rows * 32, kBlock, (int64_t)num_sms() * 32), kBlock, 0, cu(s)>>>(
-        v, tail_row, tail_start, x, ldx, alpha, beta, y, ldy, he, hv);
+    if (pl->extra_i[3] > 0) {  // empty rows before the tail tile
+        csr5_empty_rows<V, K><<<grid_for(tail_row, kBlock, (int64_t)num_sms() * 16), kBlock, 0, cu(s)>>>(
+            tail_row, A->row_offset, beta, y, ldy);
+        SSPMV_LAUNCH_CHECK();
+    }
+    csr5_rows_kernel<V, K><<<grid_for((A->f.num_rows - tail_row) * 32, kBlock, (int64_t)num_sms() * 32), kBlock, 0,
+                             cu(s)>>>(v, tail_row, tail_start, x, ldx, alpha, beta, y, ldy, he, hv);
     SSPMV_LAUNCH_CHECK();
     if (A->_p > 1) {
         csr5_fixup<V, K><<<grid_for(A->_p - 1, 256), 256, 0, cu(s)>>>(A->_p, (int64_t)A->sigma * A->omega,

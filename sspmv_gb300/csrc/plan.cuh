@@ -29,8 +29,8 @@ struct Plan {
     int kind = 0;
     MergePlan merge[2];     // [0]: tile for k <= 4, [1]: tile for k == 8
     int param = 0;          // kernel parameter set by sspmv_set_kernel (0 = library choice)
-    void *extra[8] = {nullptr};  // format-specific device buffers
-    int64_t extra_i[8] = {0};
+    void *extra[12] = {nullptr};  // format-specific device buffers
+    int64_t extra_i[12] = {0};
 };
 
 std::mutex &plan_mutex();

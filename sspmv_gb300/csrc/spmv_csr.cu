@@ -53,16 +53,20 @@ struct alignas(16) VecK {
     V v[K];
 };
 
+// One merge-path tile (split points c0, c1) of one matrix; t indexes the
+// per-tile carry slots.  Used by the single-matrix kernel (one tile per CTA)
+// and by the batched serving kernel (a CTA loops over tiles of many
+// requests); the leading barrier makes back-to-back calls safe.
 template <typename V, int K>
-__global__ void __launch_bounds__(kBlock) csr_merge_kernel(
+__device__ __forceinline__ void merge_tile(
     int m, const int32_t *__restrict__ row_offset, const int32_t *__restrict__ col_index,
     const V *__restrict__ values, const V *__restrict__ x, int64_t ldx, V alpha, V beta,
-    V *__restrict__ y, int64_t ldy, const int2 *__restrict__ coords, int32_t *__restrict__ carry_row,
-    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val) {
+    V *__restrict__ y, int64_t ldy, const int2 c0, const int2 c1, const int64_t t, int32_t *__restrict__ carry_row,
+    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val,
+    unsigned char *__restrict__ smem_raw) {
     constexpr int kItems = MergeShape<K>::items;
     constexpr int kTile = MergeShape<K>::tile;
     constexpr int kWarps = kBlock / 32;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     V *s_prod = reinterpret_cast<V *>(smem_raw);                     // kTile * K
     int *s_rowend = reinterpret_cast<int *>(s_prod + kTile * K);      // kTile + 1
     __shared__ int s_wkey[kWarps];
@@ -70,10 +74,9 @@ __global__ void __launch_bounds__(kBlock) csr_merge_kernel(
     __shared__ V s_wpref[kWarps][K];
     __shared__ V s_full[kBlock][K];
     __shared__ int s_row0_start;
+    __syncthreads();
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int64_t t = blockIdx.x;
-    const int2 c0 = coords[t], c1 = coords[t + 1];
     const int i0 = c0.x, j0 = c0.y;
     const int nrows = c1.x - i0, nnzs = c1.y - j0;
 
@@ -209,6 +212,18 @@ __global__ void __launch_bounds__(kBlock) csr_merge_kernel(
 #pragma unroll
         for (int r = 0; r < K; r++) cp[r] = sum[r];
     }
+}
+
+template <typename V, int K>
+__global__ void __launch_bounds__(kBlock) csr_merge_kernel(
+    int m, const int32_t *__restrict__ row_offset, const int32_t *__restrict__ col_index,
+    const V *__restrict__ values, const V *__restrict__ x, int64_t ldx, V alpha, V beta,
+    V *__restrict__ y, int64_t ldy, const int2 *__restrict__ coords, int32_t *__restrict__ carry_row,
+    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int64_t t = blockIdx.x;
+    merge_tile<V, K>(m, row_offset, col_index, values, x, ldx, alpha, beta, y, ldy, coords[t], coords[t + 1], t,
+                     carry_row, has_end, carry_val, head_val, smem_raw);
 }
 
 // Finishes rows that cross tile boundaries: the tile where such a row starts

@@ -135,11 +135,16 @@ def main() -> None:
                     "shapes": {k: list(v.shape) for k, v in out.items() if isinstance(v, np.ndarray)},
                     "scalars": {k: int(v) for k, v in out.items() if not isinstance(v, np.ndarray)},
                 }
+            # The reference's BSR kernel reads x up to the end of the last block
+            # column (src/spmv_bsr.cpp:148), past num_cols when it is not a
+            # multiple of the block width: give it zero padding to read.
+            x_pad = np.zeros(A.num_cols + 64, dt)
+            x_pad[:A.num_cols] = x
             for fmt, flag in SPMV:
                 if fmt == "dia" and ref_dia_too_wide(ref, A):
                     continue
                 y = y0.copy()
-                ref.spmv(fmt, flag, A, ALPHA, x, BETA, y)
+                ref.spmv(fmt, flag, A, ALPHA, x_pad, BETA, y)
                 arrays[f"y_{fmt}_{flag}"] = y
                 rec["spmv"].append([fmt, flag])
             if name == "dups":
