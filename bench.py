@@ -52,6 +52,8 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (library defaults)")
     ap.add_argument("--csr-kernel", default="", help="pin the CSR kernel as FLAG:PARAM (implies no tuning of CSR)")
+    ap.add_argument("--no-large", action="store_true", help="skip the power-law 16M SELL-c-sigma vs CSR section")
+    ap.add_argument("--no-serving", action="store_true", help="skip the request-server section")
     return ap.parse_args()
 
 
@@ -276,6 +278,19 @@ def run_gpu(args, rank, world):
     if rank == 0 and world == 1:
         cpu = cpu_baseline(hosts, families, dtypes, fmts, budget_s=15.0)
         log("cpu baseline done")
+    for c in cases:
+        if c["M"] is not c["csr"]:
+            c["M"].delete()
+    for c in cases:
+        c["csr"].delete()
+    del cases, hosts
+    large = serving = None
+    if rank == 0 and not args.no_large and args.scale == 1.0:
+        large = run_large(dev, peak)
+        log("large done")
+    if rank == 0 and not args.no_serving and args.scale == 1.0:
+        serving = run_serving()
+        log("serving done")
     return {
         "metric": "SpMV GB/s (algorithmic bytes / kernel time), all formats x 4 families x {f64,f32}",
         "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -286,7 +301,7 @@ def run_gpu(args, rank, world):
                    "alpha": 1.0, "beta": 0.0, "k_rhs": 1, "index": "int32", "parallelism": f"replicas{world}",
                    "skipped": skipped, "scale": args.scale},
         "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches),
-        "wall_s": round(wall, 3), "per_format": per_case,
+        "wall_s": round(wall, 3), "per_format": per_case, "large_powerlaw_16M": large, "serving": serving,
     }
 
 
@@ -324,6 +339,108 @@ def run_e2e(args, cases, flush, stream, world):
     step_ms = _max_over_ranks(total_ms / args.steps, world)
     return {"value": round(total_bytes / args.steps * world / (step_ms * 1e6), 1), "unit": "GB/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": round(step_ms, 4)}
+
+
+# ------------------------------------------------ large power-law section --
+def fp64_row_check(A, X, Y, rows):
+    """Normalised error of GPU rows Y[rows] against an FP64 product on the
+    same (possibly FP32-rounded) inputs: |y - y64| / (8 nnz_i eps sum|a x|)."""
+    import scipy.sparse as sp
+    m = A.num_rows
+    Asp = sp.csr_matrix((A.values.astype(np.float64), A.col_index, A.row_offset), shape=(m, A.num_cols))[rows]
+    X64 = X.astype(np.float64).reshape(A.num_cols, -1)
+    y64 = Asp @ X64
+    absum = abs(Asp) @ np.abs(X64)
+    nz = np.diff(A.row_offset)[rows].astype(np.float64)[:, None]
+    eps = np.finfo(A.values.dtype).eps
+    bound = 8.0 * np.maximum(nz, 1.0) * eps * absum + np.finfo(np.float64).tiny
+    err = np.abs(Y.reshape(len(rows), -1).astype(np.float64) - y64) / bound
+    return float(err.max(initial=0.0)), float(np.median(err))
+
+
+def run_large(dev, peak):
+    """Power-law N=16M (Zipf 2.0, mean 16, cap 50k), FP32 values, int32
+    indices: SELL-c-sigma autotuned over C in {8,16,32} x sigma in {256,
+    4096, N} against CSR (autotuned kernel), k = 1 and k = 8 right-hand
+    sides; GB/s (algorithmic bytes / kernel time, L2 flushed), fraction of the
+    measured HBM peak, and FP64 error on every 64th row."""
+    import torch
+    from sspmv_gb300 import autotune, synth
+    from sspmv_gb300 import lespmv as L
+    t0 = time.perf_counter()
+    A = synth.generate(synth.WORKLOADS["powerlaw_16M"](), 1, np.float32)
+    log(f"large: generated N={A.num_rows} nnz={A.nnz} ({time.perf_counter() - t0:.1f}s)")
+    csr = L.csr_from_host(A)
+    n, m = A.num_cols, A.num_rows
+    x1 = torch.from_numpy(synth.vector(n, 0, np.float32)).to(dev)
+    y1 = torch.zeros(m, dtype=torch.float32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    out = {"workload": "powerlaw_16M f32 (Zipf 2.0, mean 16, cap 50k)", "num_rows": m, "nnz": A.nnz, "formats": {}}
+    res_csr = autotune.tune_format(csr, x1, y1)
+    sig_n = -(-m // 32) * 32
+    cands = [dict(slicewidth=sg, chunkwidth=c, alignment=0) for c in (8, 16, 32) for sg in (256, 4096, sig_n)]
+    best = None
+    table = []
+    for kw in cands:
+        M = L.csr_to_sell_c_sigma(csr, **kw)
+        ms = autotune.time_spmv(M, x1, y1, reps=5, flush=flush)
+        table.append({"C": kw["chunkwidth"], "sigma": kw["slicewidth"], "ms": round(ms, 4)})
+        if best is None or ms < best[1]:
+            if best:
+                best[0].delete()
+            best = (M, ms, kw)
+        else:
+            M.delete()
+    scs = best[0]
+    out["sell_c_sigma_tuning"] = table
+    log(f"large: tuned SELL-c-sigma C={best[2]['chunkwidth']} sigma={best[2]['slicewidth']}")
+    rows = np.arange(0, m, 64)
+    for name, M, tuned in (("csr", csr, res_csr["best"] if res_csr else None),
+                           ("sell_c_sigma", scs, {"C": best[2]["chunkwidth"], "sigma": best[2]["slicewidth"]})):
+        rec = {"tuned": tuned}
+        for k in (1, 8):
+            X = torch.from_numpy(synth.vector(n, 0, np.float32, k).reshape(n, k)).to(dev)
+            Y = torch.zeros((m, k), dtype=torch.float32, device=dev)
+            ts = []
+            for i in range(6):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                L.spmm(1.0, M, X, 0.0, Y)
+                e1.record()
+                e1.synchronize()
+                if i >= 1:
+                    ts.append(e0.elapsed_time(e1))
+            ms = statistics.median(ts)
+            b = M.algorithmic_bytes(k, False)
+            Yh = Y[torch.from_numpy(rows).to(dev)].cpu().numpy()
+            mx, med = fp64_row_check(A, X.cpu().numpy(), Yh, rows)
+            rec[f"k{k}"] = {"ms": round(ms, 4), "GBps": round(b / ms / 1e6, 1),
+                            "GFLOPs": round(2.0 * A.nnz * k / ms / 1e6, 1),
+                            "frac_of_measured_peak": round(b / ms / 1e6 / peak, 4),
+                            "max_norm_err": round(mx, 4), "median_norm_err": round(med, 4),
+                            "within_tolerance": mx <= 1.0}
+            del X, Y
+        out["formats"][name] = rec
+        log(f"large: {name} {rec}")
+    scs.delete()
+    csr.delete()
+    out["sell_vs_csr_speedup"] = {f"k{k}": round(out["formats"]["csr"][f"k{k}"]["ms"] /
+                                                 out["formats"]["sell_c_sigma"][f"k{k}"]["ms"], 3) for k in (1, 8)}
+    out["wall_s"] = round(time.perf_counter() - t0, 1)
+    return out
+
+
+def run_serving():
+    """The request server on its serving workload (64 matrices x FP64/FP32),
+    pinned-host and device buffers: saturation throughput and p50/p99 under
+    Poisson load, batched vs one launch per request."""
+    from sspmv_gb300 import serving
+    out = {}
+    for kind, dev_buf in (("host", False), ("device", True)):
+        r = serving.serving_benchmark(64, device_buffers=dev_buf, log=log)
+        out[kind] = r
+    return out
 
 
 # ------------------------------------------------------------- CPU legs ----

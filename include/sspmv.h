@@ -405,6 +405,16 @@ double sspmv_algorithmic_bytes_sell_c_R(const sspmv_sell_c_R *A, int32_t k, int3
 sspmv_status sspmv_csr_features(const sspmv_csr *A, int32_t tile_blocks, double *features, int32_t *nnz_by_tiles,
                                 int32_t *uniq_rb, int32_t *uniq_cb, sspmv_stream_t stream);
 const char *sspmv_feature_name(int32_t i);
+/* The GrX tile-group features the reference specifies but leaves at -1
+ * (CalculateTilesExtraFeatures under BSR_ANA and AnalyzeTile_Group,
+ * src/sparse_features.cpp:884-1065, README "GrX_uniqR and GrX_uniqC"):
+ * out[0..3] = GrX_uniqR, GrX_uniqC, GrX_potReuseR, GrX_potReuseC over
+ * BestDimForBSR-sized tiles of a T x T grid (tile_blocks: T, 0 = 256) with
+ * groups of X = group rows / columns (0 = 64 / sizeof(value), the
+ * reference's CACHE_LINE / sizeof(ValueType)).  Entries with value 0 count as
+ * absent; a feature stays -1 when the tile is smaller than X. */
+sspmv_status sspmv_csr_grx_features(const sspmv_csr *A, int32_t tile_blocks, int32_t group, double *out,
+                                    sspmv_stream_t stream);
 
 /* ---------------- host utilities ---------------- */
 /* Matrix Market reader (utils/sparse_io.cpp:27-204: coordinate format,
@@ -454,6 +464,131 @@ int sspmv_synth_fill_f32(const sspmv_synth_params *p, uint64_t seed, const int32
 /* x_i ~ U[-1,1) from (seed, i). */
 void sspmv_synth_vector_f64(int64_t n, uint64_t seed, double *out);
 void sspmv_synth_vector_f32(int64_t n, uint64_t seed, float *out);
+
+/* ---------------- selector network (FP32) ---------------- */
+/* Kernels of the format selector's multilayer perceptron; no counterpart in
+ * the reference's C++ (its selector is a Keras model,
+ * SmartAdpter/models/SpMV_Adapter.py).  Row-major, device pointers, leading
+ * dimensions in elements.  W of a layer is out x in. */
+/* y = x W^T + b (b may be NULL), ReLU when relu != 0. */
+sspmv_status sspmv_nn_linear_forward(int32_t batch, int32_t in, int32_t out, const float *x, int32_t ldx,
+                                     const float *W, const float *b, int32_t relu, float *y, int32_t ldy,
+                                     sspmv_stream_t stream);
+/* Gradients of a layer from dy (masked in place by y > 0 when relu != 0,
+ * which needs ldy == out): dW = dy^T x, db = column sums of dy, dx = dy W
+ * (dx may be NULL). */
+sspmv_status sspmv_nn_linear_backward(int32_t batch, int32_t in, int32_t out, const float *x, int32_t ldx,
+                                      const float *W, const float *y, int32_t relu, float *dy, int32_t ldy,
+                                      float *dx, int32_t lddx, float *dW, float *db, sspmv_stream_t stream);
+/* Softmax cross-entropy of C logits per row: loss_rows[b] = -log p[label]
+ * (0 when label < 0), dlogits = (p - onehot) / batch. */
+sspmv_status sspmv_nn_softmax_xent(int32_t batch, int32_t C, const float *logits, int32_t ld, const int32_t *labels,
+                                   float *dlogits, int32_t ldd, float *loss_rows, sspmv_stream_t stream);
+/* Masked squared error: loss_rows[b] = sum_c mask (pred - target)^2 / count,
+ * dpred = weight * 2 (pred - target) mask / count; target and mask are
+ * batch x C dense. */
+sspmv_status sspmv_nn_masked_mse(int32_t batch, int32_t C, const float *pred, int32_t ld, const float *target,
+                                 const float *mask, float weight, float count, float *dpred, int32_t ldd,
+                                 float *loss_rows, sspmv_stream_t stream);
+/* Adam (bias-corrected, step >= 1); weight_decay * w is added to the
+ * gradient (L2 regularisation). */
+sspmv_status sspmv_nn_adam(int64_t n, float *w, const float *g, float *m, float *v, float lr, float beta1,
+                           float beta2, float eps, int32_t step, float weight_decay, sspmv_stream_t stream);
+
+/* ---------------- request server ---------------- */
+/* No counterpart in the reference (its benchmark_spmv_<fmt> programs run one
+ * matrix per process).  A server keeps registered matrices resident in HBM in
+ * the format each was registered with (loaded from the caller's host arrays
+ * on first use, least-recently-used eviction under a byte budget) and serves
+ * requests y = alpha * A * X + beta * Y (k right-hand sides, row-major X/Y
+ * with leading dimensions, HOST buffers) with continuous batching: while
+ * batches are on the GPU, the requests that arrive are gathered into the
+ * next one.  CSR requests with k in {1, 2, 4, 8} of a batch run in one
+ * persistent merge-path launch per (value type, k) group, replayed from a
+ * CUDA graph; other requests get their format's own launch in the same
+ * batch.  A request's result is bit-identical whatever else is batched with
+ * it.  Mode SSPMV_SERVE_PER_REQUEST serves one request at a time through
+ * sspmv_spmm_<fmt> (the plain per-request launch path, for comparison). */
+typedef enum {
+    SSPMV_FMT_CSR = 0,
+    SSPMV_FMT_COO = 1,
+    SSPMV_FMT_ELL = 2,
+    SSPMV_FMT_SELL = 3,
+    SSPMV_FMT_SELL_C_SIGMA = 4,
+    SSPMV_FMT_SELL_C_R = 5,
+    SSPMV_FMT_DIA = 6,
+    SSPMV_FMT_BSR = 7,
+    SSPMV_FMT_CSR5 = 8
+} sspmv_format;
+
+typedef enum { SSPMV_SERVE_BATCHED = 0, SSPMV_SERVE_PER_REQUEST = 1 } sspmv_serve_mode;
+
+typedef struct {
+    int32_t mode;               /* sspmv_serve_mode */
+    int32_t max_batch_requests; /* 0: 1024 */
+    int64_t max_batch_tiles;    /* merge tiles (carry slots) per batch; 0: 1 << 17 */
+    int64_t arena_bytes;        /* per batch in flight, device staging for X and for Y each; 0: 512 MiB */
+    int64_t stage_limit_bytes;  /* X / Y up to this size are packed through pinned staging; 0: 1 MiB */
+    int64_t hbm_budget_bytes;   /* resident matrices; 0: 120e9 */
+    int32_t num_inflight;       /* batches in flight, one stream each; 0: 2 */
+    int32_t use_graphs;         /* batched launches replayed from CUDA graphs */
+} sspmv_server_config;
+
+#define SSPMV_REQ_DEVICE_BUFFERS 1 /* x and y are device pointers: no copies */
+
+typedef struct {
+    int32_t matrix_id;
+    int32_t k;                  /* right-hand sides (>= 1) */
+    double alpha, beta;
+    const void *x;              /* num_cols rows of ldx values (host unless SSPMV_REQ_DEVICE_BUFFERS) */
+    int64_t ldx;
+    void *y;                    /* num_rows rows of ldy values (read when beta != 0) */
+    int64_t ldy;
+    int32_t flags;              /* SSPMV_REQ_DEVICE_BUFFERS or 0 */
+    int32_t reserved;
+} sspmv_request;
+
+typedef struct {
+    int32_t status;             /* sspmv_status of the request */
+    int32_t batch_size;         /* requests in its batch */
+    int64_t batch_id;
+    int64_t arrival_ns;         /* submit time (replay: the scheduled arrival), steady clock */
+    int64_t launch_ns;          /* its batch was issued to the GPU */
+    int64_t done_ns;            /* result in the caller's y */
+} sspmv_request_info;
+
+typedef struct {
+    int64_t requests_done, requests_failed, batches, batched_requests, batched_tiles, graph_launches;
+    int64_t loads, evictions, resident_matrices, resident_bytes;
+} sspmv_server_stats;
+
+typedef struct sspmv_server sspmv_server;
+
+sspmv_status sspmv_server_create(const sspmv_server_config *cfg, sspmv_server **out);
+/* Serves what is queued, then stops and frees everything the server holds. */
+sspmv_status sspmv_server_destroy(sspmv_server *srv);
+/* Registers matrix `id` from host CSR arrays that must stay valid while it is
+ * registered.  format: sspmv_format; params: the converter's integer
+ * arguments in declaration order (ELL: ld; SELL: chunkwidth, alignment;
+ * SELL-c-sigma: slicewidth, chunkwidth, alignment; SELL-c-R: chunkwidth,
+ * alignment; DIA: max_diags, alignment; BSR: blockDimRow, blockDimCol; CSR5:
+ * sigma, omega), NULL for the defaults. */
+sspmv_status sspmv_server_add_matrix(sspmv_server *srv, int32_t id, int32_t value_type, int64_t num_rows,
+                                     int64_t num_cols, int64_t num_nnzs, const int32_t *row_offset,
+                                     const int32_t *col_index, const void *values, int32_t format,
+                                     const int32_t *params);
+/* Loads matrix `id` into HBM now (otherwise its first request does). */
+sspmv_status sspmv_server_preload(sspmv_server *srv, int32_t id);
+/* Queues one request; x and y must stay valid until it completes. */
+sspmv_status sspmv_server_submit(sspmv_server *srv, const sspmv_request *req, int64_t *ticket);
+/* Waits (timeout_s < 0: forever) for a submitted request and forgets it;
+ * SSPMV_DEVICE_TIMEOUT if it has not completed in time. */
+sspmv_status sspmv_server_wait(sspmv_server *srv, int64_t ticket, double timeout_s, sspmv_request_info *info);
+/* Open-loop load: submits request i at arrival_ns[i] nanoseconds after the
+ * call starts (ascending), then waits for all of them and fills infos[i]. */
+sspmv_status sspmv_server_replay(sspmv_server *srv, int64_t n, const sspmv_request *reqs, const int64_t *arrival_ns,
+                                 sspmv_request_info *infos);
+sspmv_status sspmv_server_get_stats(const sspmv_server *srv, sspmv_server_stats *stats);
 
 #ifdef __cplusplus
 }

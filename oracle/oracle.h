@@ -192,6 +192,16 @@ int oracle_max_threads(void);
 void oracle_features(int32_t m, int32_t n, const int32_t *rowptr, const int32_t *col, const double *val,
                      int32_t T, double *F, int32_t *nnz_by_tiles, int32_t *uniq_rb, int32_t *uniq_cb);
 
+/* GrX tile-group features (CalculateTilesExtraFeatures under BSR_ANA and
+ * AnalyzeTile_Group, src/sparse_features.cpp:884-1065), restated with the
+ * reference's literal loops over dense BestDimForBSR-sized tiles: out[0..3] =
+ * GrX_uniqR, GrX_uniqC, GrX_potReuseR, GrX_potReuseC (-1 where the tile is
+ * smaller than X).  The reference's own code for these is not built (its
+ * BSR_ANA block does not compile), so this restatement is not pinned to
+ * reference output. */
+void oracle_grx(int32_t m, int32_t n, const int32_t *rowptr, const int32_t *col, const double *val, int32_t T,
+                int32_t X, double *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -252,6 +252,15 @@ class Oracle:
                           _ptr(F), _ptr(t), _ptr(u), _ptr(v))
         return F, {"tiles": t, "urb": u, "ucb": v}
 
+    def grx(self, csr, T=256, X=8):
+        """GrX_uniqR, GrX_uniqC, GrX_potReuseR, GrX_potReuseC of a CSR."""
+        L = self.lib
+        L.oracle_grx.argtypes = [_i32, _i32, _vp, _vp, _vp, _i32, _i32, _vp]
+        out = np.zeros(4)
+        val = np.ascontiguousarray(csr.values, np.float64)
+        L.oracle_grx(csr.num_rows, csr.num_cols, _ptr(csr.row_offset), _ptr(csr.col_index), _ptr(val), T, X, _ptr(out))
+        return out
+
     def max_rel_error(self, a, b):
         return float(getattr(self.lib, f"oracle_max_rel_error_{_sfx(a.dtype)}")(
             _ptr(a), _ptr(b), _i64(a.size)))

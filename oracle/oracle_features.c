@@ -336,3 +336,125 @@ void oracle_features(int32_t m, int32_t n, const int32_t *rowptr, const int32_t 
     free(maxc);
     free(minc);
 }
+
+/* BestDimForBSR (src/sparse_features.cpp:858-880). */
+static int64_t best_dim_for_bsr(int64_t nums, int64_t target) {
+    int64_t best = 0, best_diff = 10000;
+    for (int64_t dim = 1; dim < nums; dim++) {
+        int64_t mb = (nums + dim - 1) / dim;
+        int64_t diff = mb > target ? mb - target : target - mb;
+        if (diff < best_diff) {
+            best_diff = diff;
+            best = dim;
+        }
+        if (diff == 0) break;
+    }
+    return best > 0 ? best : 1;
+}
+
+/* AnalyzeTile_Group (src/sparse_features.cpp:884-934) on one dense R x Cd tile. */
+static void analyze_tile_group(const double *t, int64_t R, int64_t Cd, int64_t X, long long *gr, long long *gc,
+                               int flag_row, int flag_col) {
+    if (flag_row) {
+        for (int64_t bc = 0; bc < Cd; ++bc) {
+            for (int64_t br = 0; br < R; br++) {
+                if (t[br * Cd + bc] != 0) {
+                    if (br + X <= R) {
+                        int64_t step;
+                        for (step = 1; step < X; step++)
+                            if (t[(br + step) * Cd + bc] == 0) break;
+                        if (step == X) ++*gr;
+                        br += step;
+                    } else {
+                        break;
+                    }
+                }
+            }
+        }
+    }
+    if (flag_col) {
+        for (int64_t br = 0; br < R; br++) {
+            for (int64_t bc = 0; bc < Cd; ++bc) {
+                if (t[br * Cd + bc] != 0) {
+                    if (bc + X <= Cd) {
+                        int64_t step;
+                        for (step = 1; step < X; step++)
+                            if (t[br * Cd + bc + step] == 0) break;
+                        if (step == X) ++*gc;
+                        bc += step;
+                    } else {
+                        break;
+                    }
+                }
+            }
+        }
+    }
+}
+
+void oracle_grx(int32_t m, int32_t n, const int32_t *rowptr, const int32_t *col, const double *val, int32_t T,
+                int32_t X, double *out) {
+    const int64_t R = best_dim_for_bsr(m, T), Cd = best_dim_for_bsr(n, T);
+    const int64_t mb = (m + R - 1) / R, nb = (n + Cd - 1) / Cd;
+    const int flag_r = R >= X, flag_c = Cd >= X;
+    const int64_t gpr = flag_r ? (R + X - 1) / X : 0, gpc = flag_c ? (Cd + X - 1) / X : 0;
+    const int64_t nnz = rowptr[m];
+    long long gr = 0, gc = 0;
+    long long *pot_r = (long long *)calloc((size_t)(mb * gpr + 1), sizeof(long long));
+    long long *pot_c = (long long *)calloc((size_t)(nb * gpc + 1), sizeof(long long));
+    double *tile = (double *)calloc((size_t)(R * Cd), sizeof(double));
+    char *seen = (char *)calloc((size_t)nb, 1);
+    int64_t *touched = (int64_t *)malloc(sizeof(int64_t) * (size_t)nb);
+    char *fr = (char *)malloc((size_t)(gpr + 1)), *fc = (char *)malloc((size_t)(gpc + 1));
+    for (int64_t i = 0; i < mb; i++) {
+        const int64_t r0 = i * R, r1 = r0 + R < m ? r0 + R : m;
+        int64_t nt = 0;
+        for (int64_t r = r0; r < r1; r++)
+            for (int64_t q = rowptr[r]; q < rowptr[r + 1]; q++) {
+                const int64_t j = col[q] / Cd;
+                if (!seen[j]) {
+                    seen[j] = 1;
+                    touched[nt++] = j;
+                }
+            }
+        for (int64_t u = 0; u < nt; u++) {
+            const int64_t j = touched[u];
+            seen[j] = 0;
+            for (int64_t r = r0; r < r1; r++)
+                for (int64_t q = rowptr[r]; q < rowptr[r + 1]; q++)
+                    if (col[q] / Cd == j) tile[(r - r0) * Cd + (col[q] - j * Cd)] = val[q];
+            /* potReuse flags: one count per tile for each row / column group holding a nonzero (:1030-1042) */
+            memset(fr, 1, (size_t)(gpr + 1));
+            memset(fc, 1, (size_t)(gpc + 1));
+            for (int64_t br = 0; br < R; br++)
+                for (int64_t bc = 0; bc < Cd; bc++)
+                    if (tile[br * Cd + bc] != 0) {
+                        if (flag_r && fr[br / X]) {
+                            pot_r[i * gpr + br / X]++;
+                            fr[br / X] = 0;
+                        }
+                        if (flag_c && fc[bc / X]) {
+                            pot_c[j * gpc + bc / X]++;
+                            fc[bc / X] = 0;
+                        }
+                    }
+            analyze_tile_group(tile, R, Cd, X, &gr, &gc, flag_r, flag_c);
+            for (int64_t r = r0; r < r1; r++)
+                for (int64_t q = rowptr[r]; q < rowptr[r + 1]; q++)
+                    if (col[q] / Cd == j) tile[(r - r0) * Cd + (col[q] - j * Cd)] = 0;
+        }
+    }
+    long long sr = 0, sc = 0;
+    for (int64_t k = 0; k < mb * gpr; k++) sr += pot_r[k];
+    for (int64_t k = 0; k < nb * gpc; k++) sc += pot_c[k];
+    out[0] = flag_r ? (double)gr / (double)nnz : -1.0;
+    out[1] = flag_c ? (double)gc / (double)nnz : -1.0;
+    out[2] = flag_r ? (double)sr / (double)(mb * gpr) : -1.0;
+    out[3] = flag_c ? (double)sc / (double)(nb * gpc) : -1.0;
+    free(pot_r);
+    free(pot_c);
+    free(tile);
+    free(seen);
+    free(touched);
+    free(fr);
+    free(fc);
+}

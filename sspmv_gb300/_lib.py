@@ -173,7 +173,52 @@ _SIGS["sspmv_coo_to_csr"] = (_st, [C.POINTER(Coo), C.POINTER(Csr), _vp])
 _SIGS["sspmv_csr_count_blocks"] = (_st, [C.POINTER(Csr), _i32, _i32, C.POINTER(_i64), _vp])
 _SIGS["sspmv_csr_features"] = (_st, [C.POINTER(Csr), _i32, _vp, _vp, _vp, _vp, _vp])
 _SIGS["sspmv_feature_name"] = (C.c_char_p, [_i32])
+_SIGS["sspmv_csr_grx_features"] = (_st, [C.POINTER(Csr), _i32, _i32, _vp, _vp])
 NUM_FEATURES = 62
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("max_batch_requests", C.c_int32), ("max_batch_tiles", C.c_int64),
+                ("arena_bytes", C.c_int64), ("stage_limit_bytes", C.c_int64), ("hbm_budget_bytes", C.c_int64),
+                ("num_inflight", C.c_int32), ("use_graphs", C.c_int32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("matrix_id", C.c_int32), ("k", C.c_int32), ("alpha", C.c_double), ("beta", C.c_double),
+                ("x", C.c_void_p), ("ldx", C.c_int64), ("y", C.c_void_p), ("ldy", C.c_int64),
+                ("flags", C.c_int32), ("reserved", C.c_int32)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int32), ("batch_size", C.c_int32), ("batch_id", C.c_int64),
+                ("arrival_ns", C.c_int64), ("launch_ns", C.c_int64), ("done_ns", C.c_int64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("requests_done", "requests_failed", "batches", "batched_requests",
+                                         "batched_tiles", "graph_launches", "loads", "evictions",
+                                         "resident_matrices", "resident_bytes")]
+
+
+_f = C.c_float
+_SIGS.update({
+    "sspmv_nn_linear_forward": (_st, [_i32, _i32, _i32, _vp, _i32, _vp, _vp, _i32, _vp, _i32, _vp]),
+    "sspmv_nn_linear_backward": (_st, [_i32, _i32, _i32, _vp, _i32, _vp, _vp, _i32, _vp, _i32, _vp, _i32, _vp, _vp,
+                                       _vp]),
+    "sspmv_nn_softmax_xent": (_st, [_i32, _i32, _vp, _i32, _vp, _vp, _i32, _vp, _vp]),
+    "sspmv_nn_masked_mse": (_st, [_i32, _i32, _vp, _i32, _vp, _vp, _f, _f, _vp, _i32, _vp, _vp]),
+    "sspmv_nn_adam": (_st, [_i64, _vp, _vp, _vp, _vp, _f, _f, _f, _f, _i32, _f, _vp]),
+})
+_SIGS.update({
+    "sspmv_server_create": (_st, [C.POINTER(ServerConfig), C.POINTER(_vp)]),
+    "sspmv_server_destroy": (_st, [_vp]),
+    "sspmv_server_add_matrix": (_st, [_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp]),
+    "sspmv_server_preload": (_st, [_vp, _i32]),
+    "sspmv_server_submit": (_st, [_vp, C.POINTER(Request), C.POINTER(_i64)]),
+    "sspmv_server_wait": (_st, [_vp, _i64, _d, C.POINTER(RequestInfo)]),
+    "sspmv_server_replay": (_st, [_vp, _i64, _vp, _vp, _vp]),
+    "sspmv_server_get_stats": (_st, [_vp, C.POINTER(ServerStats)]),
+})
 
 for _n, (_r, _a) in _SIGS.items():
     register(_n, _r, _a)

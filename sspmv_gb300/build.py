@@ -77,6 +77,31 @@ def build_library(verbose: bool = False, extra: list[str] | None = None, jobs: i
     return LIB
 
 
+CLI_SRC = PKG / "cli" / "benchmark_spmv.cpp"
+BINDIR = PKG / "bin"
+CLI_FORMATS = ("csr", "coo", "ell", "sell", "sell_c_sigma", "sell_c_R", "dia", "bsr", "csr5")
+
+
+def build_cli() -> Path:
+    """sspmv_gb300/bin/benchmark_spmv (links libsspmv.so by rpath) and the
+    benchmark_spmv_<fmt> names the reference's programs have."""
+    BINDIR.mkdir(exist_ok=True)
+    exe = BINDIR / "benchmark_spmv"
+    if not exe.exists() or exe.stat().st_mtime < max(CLI_SRC.stat().st_mtime, LIB.stat().st_mtime):
+        cmd = [NVCC, "-O2", "-std=c++17", f"-I{ROOT / 'include'}", "-x", "c++", str(CLI_SRC), "-o", str(exe),
+               f"-L{LIBDIR}", "-lsspmv", "-lcudart", "-Xlinker", "-rpath=$ORIGIN/../lib"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"cli build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    for f in CLI_FORMATS:
+        link = BINDIR / f"benchmark_spmv_{f}"
+        if not link.is_symlink():
+            if link.exists():
+                link.unlink()
+            link.symlink_to("benchmark_spmv")
+    return exe
+
+
 def build_oracle(with_reference: bool | None = None) -> None:
     """CPU oracle (test infrastructure): oracle/liboracle.so, plus the
     reference harness oracle/_ref/libref.so when the reference sources exist."""
@@ -91,4 +116,5 @@ def build_oracle(with_reference: bool | None = None) -> None:
 
 if __name__ == "__main__":
     print(build_library(verbose=True))
+    print(build_cli())
     build_oracle()

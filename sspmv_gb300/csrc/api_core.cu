@@ -14,6 +14,13 @@ static std::atomic<long long> g_launches{0};
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+static thread_local int g_delete_nosync = 0;
+DeleteWithoutDeviceSync::DeleteWithoutDeviceSync() { g_delete_nosync++; }
+DeleteWithoutDeviceSync::~DeleteWithoutDeviceSync() { g_delete_nosync--; }
+void delete_barrier() {
+    if (g_delete_nosync == 0) cudaDeviceSynchronize();
+}
+
 void set_error(const char *fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
@@ -182,7 +189,7 @@ extern "C" sspmv_status sspmv_delete_csr(sspmv_csr *A) {
     if (!A) return SSPMV_OK;
     // The matrix may still be in use on any stream: wait for the device
     // before returning its memory.
-    cudaDeviceSynchronize();
+    delete_barrier();
     free_plan(&A->f, nullptr);
     if (A->f.owns) {
         dfree(A->row_offset, nullptr);

@@ -327,7 +327,7 @@ extern "C" sspmv_status sspmv_bsr_export(const sspmv_bsr *A, int32_t *row_ptr, i
 
 extern "C" sspmv_status sspmv_delete_bsr(sspmv_bsr *A) {
     if (!A) return SSPMV_OK;
-    cudaDeviceSynchronize();
+    delete_barrier();
     free_plan(&A->f, nullptr);
     if (A->f.owns) {
         dfree(A->row_ptr, nullptr);

@@ -56,6 +56,16 @@ inline void dfree(void *p, sspmv_stream_t s) {
     if (p) cudaFreeAsync(p, cu(s));
 }
 
+// sspmv_delete_<fmt> waits for the whole device before freeing (the matrix
+// may still be in use on any stream).  A caller that knows no queued work
+// uses the matrix any more (the request server, after the matrix's last
+// batch completed) opens this scope on its thread to skip that wait.
+struct DeleteWithoutDeviceSync {
+    DeleteWithoutDeviceSync();
+    ~DeleteWithoutDeviceSync();
+};
+void delete_barrier();
+
 inline size_t vsize(int32_t vt) { return vt == SSPMV_F64 ? 8 : 4; }
 inline int default_alignment(int32_t vt) { return 64 / (int)vsize(vt); }  // SIMD_WIDTH/8/sizeof(V)
 

@@ -272,7 +272,9 @@ __global__ void __launch_bounds__(kBlock) coo_tile_kernel(
 // carries the open row into the next step.  A lane whose nonzero is the last
 // of its row writes that row -- unless the row began before the warp's chunk
 // (head piece) -- and the chunk's open last row is left as a carry.  No
-// shared memory, no barriers.
+// shared memory, no barriers.  The loads of kBatch steps (row, column, value,
+// then the x gathers) are issued before any of them is scanned, so each lane
+// keeps kBatch independent gathers in flight.
 constexpr int kWarpChunk = 256;
 
 template <typename V, int K>
@@ -281,6 +283,8 @@ __global__ void __launch_bounds__(kBlock) coo_warp_kernel(
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
     int32_t *__restrict__ carry_row, int32_t *__restrict__ has_end, V *__restrict__ carry_val,
     V *__restrict__ head_val) {
+    constexpr int kSteps = kWarpChunk / 32;
+    constexpr int kBatch = K <= 2 ? kSteps : K <= 4 ? 4 : 2;
     const int lane = threadIdx.x & 31;
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t j0 = w * kWarpChunk;
@@ -293,56 +297,72 @@ __global__ void __launch_bounds__(kBlock) coo_warp_kernel(
 #pragma unroll
     for (int q = 0; q < K; q++) carry[q] = V(0);
     bool first_ended = false;
-    for (int64_t base = j0; base < j1; base += 32) {
-        const int64_t e = base + lane;
-        const bool valid = e < j1;
-        int r = -1 - lane;  // unique keys for idle lanes
-        V p[K];
+    for (int s0 = 0; s0 < kSteps; s0 += kBatch) {
+        if (j0 + (int64_t)s0 * 32 >= j1) break;
+        int rr[kBatch], cc[kBatch];
+        V aa[kBatch];
 #pragma unroll
-        for (int q = 0; q < K; q++) p[q] = V(0);
-        if (valid) {
-            r = ld_stream(ri + e);
-            const int c = ld_stream(ci + e);
-            const V a = ld_stream(cv + e);
-#pragma unroll
-            for (int q = 0; q < K; q++) p[q] = a * ld_x(x + (int64_t)c * ldx + q);
-        }
-        if (lane == 0 && r == carry_r) {
-#pragma unroll
-            for (int q = 0; q < K; q++) p[q] += carry[q];
-        }
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int r2 = __shfl_up_sync(0xffffffffu, r, o);
-            V v2[K];
-#pragma unroll
-            for (int q = 0; q < K; q++) v2[q] = __shfl_up_sync(0xffffffffu, p[q], o);
-            if (lane >= o && r2 == r) {
-#pragma unroll
-                for (int q = 0; q < K; q++) p[q] += v2[q];
+        for (int u = 0; u < kBatch; u++) {
+            const int64_t e = j0 + (int64_t)(s0 + u) * 32 + lane;
+            rr[u] = -1 - lane;  // unique keys for idle lanes
+            cc[u] = -1;
+            aa[u] = V(0);
+            if (e < j1) {
+                rr[u] = ld_stream(ri + e);
+                cc[u] = ld_stream(ci + e);
+                aa[u] = ld_stream(cv + e);
             }
         }
-        // row of the next nonzero in the matrix
-        int rn = __shfl_down_sync(0xffffffffu, r, 1);
-        if (valid && (lane == 31 || e + 1 >= j1)) rn = e + 1 < nnz ? __ldg(ri + e + 1) : -1;
-        const bool ends = valid && rn != r;
-        if (ends) {
-            if (r == first_row && head_open) {
-                V *hp = head_val + w * kMaxK;
+        V pp[kBatch][K];
 #pragma unroll
-                for (int q = 0; q < K; q++) hp[q] = p[q];
-            } else {
-                V *yp = y + (int64_t)r * ldy;
+        for (int u = 0; u < kBatch; u++)
 #pragma unroll
-                for (int q = 0; q < K; q++) yp[q] = axpby(alpha, p[q], beta, yp + q);
+            for (int q = 0; q < K; q++) pp[u][q] = cc[u] >= 0 ? aa[u] * ld_x(x + (int64_t)cc[u] * ldx + q) : V(0);
+#pragma unroll
+        for (int u = 0; u < kBatch; u++) {
+            const int64_t base = j0 + (int64_t)(s0 + u) * 32;
+            if (base >= j1) break;
+            const int64_t e = base + lane;
+            const bool valid = e < j1;
+            const int r = rr[u];
+            V *p = pp[u];
+            if (lane == 0 && r == carry_r) {
+#pragma unroll
+                for (int q = 0; q < K; q++) p[q] += carry[q];
             }
-        }
-        if (__any_sync(0xffffffffu, ends && r == first_row)) first_ended = true;
-        // open row at the end of this step -> next step / next chunk
-        const int last = (int)min((int64_t)31, j1 - 1 - base);
-        carry_r = __shfl_sync(0xffffffffu, ends ? -2 : r, last);
 #pragma unroll
-        for (int q = 0; q < K; q++) carry[q] = __shfl_sync(0xffffffffu, p[q], last);
+            for (int o = 1; o < 32; o <<= 1) {
+                const int r2 = __shfl_up_sync(0xffffffffu, r, o);
+                V v2[K];
+#pragma unroll
+                for (int q = 0; q < K; q++) v2[q] = __shfl_up_sync(0xffffffffu, p[q], o);
+                if (lane >= o && r2 == r) {
+#pragma unroll
+                    for (int q = 0; q < K; q++) p[q] += v2[q];
+                }
+            }
+            // row of the next nonzero in the matrix
+            int rn = __shfl_down_sync(0xffffffffu, r, 1);
+            if (valid && (lane == 31 || e + 1 >= j1)) rn = e + 1 < nnz ? __ldg(ri + e + 1) : -1;
+            const bool ends = valid && rn != r;
+            if (ends) {
+                if (r == first_row && head_open) {
+                    V *hp = head_val + w * kMaxK;
+#pragma unroll
+                    for (int q = 0; q < K; q++) hp[q] = p[q];
+                } else {
+                    V *yp = y + (int64_t)r * ldy;
+#pragma unroll
+                    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, p[q], beta, yp + q);
+                }
+            }
+            if (__any_sync(0xffffffffu, ends && r == first_row)) first_ended = true;
+            // open row at the end of this step -> next step / next chunk
+            const int last = (int)min((int64_t)31, j1 - 1 - base);
+            carry_r = __shfl_sync(0xffffffffu, ends ? -2 : r, last);
+#pragma unroll
+            for (int q = 0; q < K; q++) carry[q] = __shfl_sync(0xffffffffu, p[q], last);
+        }
     }
     if (lane == 0) {
         has_end[w] = first_ended ? 1 : 0;
@@ -665,7 +685,7 @@ extern "C" sspmv_status sspmv_coo_export(const sspmv_coo *A, int32_t *row_index,
 
 extern "C" sspmv_status sspmv_delete_coo(sspmv_coo *A) {
     if (!A) return SSPMV_OK;
-    cudaDeviceSynchronize();
+    delete_barrier();
     free_plan(&A->f, nullptr);
     if (A->f.owns) {
         dfree(A->row_index, nullptr);

@@ -701,7 +701,7 @@ extern "C" sspmv_status sspmv_csr5_export(const sspmv_csr5 *A, uint32_t *tile_pt
 
 extern "C" sspmv_status sspmv_delete_csr5(sspmv_csr5 *A) {
     if (!A) return SSPMV_OK;
-    cudaDeviceSynchronize();
+    delete_barrier();
     free_plan(&A->f, nullptr);
     if (A->f.owns) {
         dfree(A->row_offset, nullptr);

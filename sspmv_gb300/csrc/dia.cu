@@ -250,7 +250,7 @@ extern "C" sspmv_status sspmv_dia_export(const sspmv_dia *A, int64_t *diag_offse
 
 extern "C" sspmv_status sspmv_delete_dia(sspmv_dia *A) {
     if (!A) return SSPMV_OK;
-    cudaDeviceSynchronize();
+    delete_barrier();
     free_plan(&A->f, nullptr);
     if (A->f.owns) {
         dfree(A->diag_offsets, nullptr);

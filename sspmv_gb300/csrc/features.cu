@@ -354,6 +354,193 @@ sspmv_status int_stats(const int32_t *d, int64_t len, double mean, VecStats *r, 
 
 }  // namespace
 
+// ------------------------------------------------------------ GrX features --
+// The tile group analysis the reference specifies but does not build
+// (CalculateTilesExtraFeatures under BSR_ANA and AnalyzeTile_Group,
+// src/sparse_features.cpp:884-1065): tiles are R x Cd blocks with R =
+// BestDimForBSR(num_rows, T), Cd = BestDimForBSR(num_cols, T); an entry is
+// present when its value is nonzero.
+//   GrX_uniqC: inside each tile, each row is scanned left to right; at a
+//     present column p with p + X <= Cd the scan counts a group when columns
+//     p .. p+X-1 are all present and resumes at p + step + 1.  For a run of L
+//     consecutive present columns inside one tile this counts
+//     (L >= X) ? (L - X) / (X + 1) + 1 : 0 groups.  GrX_uniqR likewise down
+//     each column.  Both are divided by num_nnzs.
+//   GrX_potReuseR: number of (X-row group of a tile row, tile column) pairs
+//     holding a present entry, divided by mb * ceil(R / X); GrX_potReuseC
+//     likewise with column groups and tile rows.
+// A feature stays -1 when the tile is smaller than X in its direction.
+namespace {
+
+int64_t best_dim_for_tiles(int64_t nums, int64_t target) {
+    // BestDimForBSR (src/sparse_features.cpp:858-880): the first Dim whose
+    // block count ceil(nums / Dim) is closest to target.
+    int64_t best = 0, best_diff = 10000;
+    for (int64_t dim = 1; dim < nums; dim++) {
+        const int64_t mb = (nums + dim - 1) / dim;
+        const int64_t diff = mb > target ? mb - target : target - mb;
+        if (diff < best_diff) {
+            best_diff = diff;
+            best = dim;
+        }
+        if (diff == 0) break;
+        if (mb < target && diff >= best_diff) break;  // block counts only fall from here on
+    }
+    return best > 0 ? best : 1;
+}
+
+template <typename V>
+__global__ void grx_keys(int64_t m, int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
+                         const V *__restrict__ val, uint64_t sentinel, uint64_t *__restrict__ k_rc,
+                         uint64_t *__restrict__ k_cr, uint32_t *__restrict__ v1, uint32_t *__restrict__ v2) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        for (int64_t jj = rp[i]; jj < rp[i + 1]; jj++) {
+            const bool present = val[jj] != V(0);
+            const uint64_t c = (uint64_t)ci[jj];
+            k_rc[jj] = present ? (uint64_t)i * (uint64_t)n + c : sentinel;
+            k_cr[jj] = present ? c * (uint64_t)m + (uint64_t)i : sentinel;
+            v1[jj] = v2[jj] = 0;
+        }
+}
+
+// Groups in runs of consecutive minor indices (keys sorted, major * minor_n + minor).
+__global__ void grx_runs(int64_t cnt, const uint64_t *__restrict__ k, uint64_t sentinel, uint64_t minor_n,
+                         uint64_t tile, int64_t X, unsigned long long *__restrict__ total) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t key = k[q];
+        if (key == sentinel || (q > 0 && k[q - 1] == key)) continue;
+        if (q > 0 && (key % minor_n) % tile != 0 && k[q - 1] == key - 1) continue;  // not the start of a run
+        int64_t L = 1;
+        uint64_t last = key;
+        for (int64_t j = q + 1; j < cnt; j++) {
+            const uint64_t kj = k[j];
+            if (kj == last) continue;
+            if (kj == sentinel || kj != last + 1 || (kj % minor_n) % tile == 0) break;
+            last = kj;
+            L++;
+        }
+        if (L >= X) atomicAdd(total, (unsigned long long)((L - X) / (X + 1) + 1));
+    }
+}
+
+// (group of X majors inside its tile, tile of the minor index) keys.
+__global__ void grx_pot_keys(int64_t cnt, const uint64_t *__restrict__ k, uint64_t sentinel, uint64_t minor_n,
+                             uint64_t tile_major, uint64_t tile_minor, uint64_t X, uint64_t groups_per_tile,
+                             uint64_t ntiles_minor, uint64_t out_sentinel, uint64_t *__restrict__ out) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t key = k[q];
+        if (key == sentinel) {
+            out[q] = out_sentinel;
+            continue;
+        }
+        const uint64_t maj = key / minor_n, mnr = key % minor_n;
+        const uint64_t group = (maj / tile_major) * groups_per_tile + (maj % tile_major) / X;
+        out[q] = group * ntiles_minor + mnr / tile_minor;
+    }
+}
+
+__global__ void count_distinct(int64_t cnt, const uint64_t *__restrict__ k, uint64_t sentinel,
+                               unsigned long long *__restrict__ total) {
+    unsigned long long c = 0;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += (int64_t)gridDim.x * blockDim.x)
+        c += k[q] != sentinel && (q == 0 || k[q - 1] != k[q]);
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(total, c);
+}
+
+}  // namespace
+
+extern "C" sspmv_status sspmv_csr_grx_features(const sspmv_csr *A, int32_t tile_blocks, int32_t group, double *out,
+                                               sspmv_stream_t s) {
+    if (!A || !out) return fail(SSPMV_INVALID_ARG, "null argument");
+    SSPMV_TRY(check_dims(A->f.value_type, A->f.num_rows, A->f.num_cols, A->f.num_nnzs));
+    const int64_t m = A->f.num_rows, n = A->f.num_cols, nnz = A->f.num_nnzs;
+    if (m == 0 || n == 0 || nnz == 0) return fail(SSPMV_INVALID_ARG, "features need a nonempty matrix");
+    if (tile_blocks < 0 || group < 0) return fail(SSPMV_INVALID_ARG, "negative tile_blocks or group");
+    const int64_t T = tile_blocks > 0 ? tile_blocks : 256;
+    const int64_t X = group > 0 ? group : 64 / (int64_t)vsize(A->f.value_type);
+    const int64_t R = best_dim_for_tiles(m, T), Cd = best_dim_for_tiles(n, T);
+    const int64_t mb = (m + R - 1) / R, nb = (n + Cd - 1) / Cd;
+    const bool do_r = R >= X, do_c = Cd >= X;
+    for (int i = 0; i < 4; i++) out[i] = -1.0;
+    if (!do_r && !do_c) return SSPMV_OK;
+    uint64_t *k_rc = nullptr, *k_cr = nullptr, *k_pot = nullptr;
+    uint32_t *v1 = nullptr, *v2 = nullptr, *v3 = nullptr;
+    unsigned long long *cnt = nullptr;
+    auto release = [&]() {
+        dfree(k_rc, s); dfree(k_cr, s); dfree(k_pot, s); dfree(v1, s); dfree(v2, s); dfree(v3, s); dfree(cnt, s);
+    };
+    sspmv_status st = SSPMV_OK;
+#define GTRY(x)                          \
+    do {                                 \
+        st = (x);                        \
+        if (st != SSPMV_OK) {            \
+            release();                   \
+            return st;                   \
+        }                                \
+    } while (0)
+    GTRY(dalloc(&k_rc, (size_t)nnz, s));
+    GTRY(dalloc(&k_cr, (size_t)nnz, s));
+    GTRY(dalloc(&k_pot, (size_t)nnz, s));
+    GTRY(dalloc(&v1, (size_t)nnz, s));
+    GTRY(dalloc(&v2, (size_t)nnz, s));
+    GTRY(dalloc(&v3, (size_t)nnz, s));
+    GTRY(dalloc(&cnt, 4, s));
+    cudaMemsetAsync(cnt, 0, 32, cu(s));
+    const uint64_t sentinel = (uint64_t)m * (uint64_t)n;
+    const unsigned gm = grid_for(m, 256, (int64_t)num_sms() * 8), gz = grid_for(nnz, 256, (int64_t)num_sms() * 16);
+    GTRY(dispatch_value(A->f.value_type, [&](auto tag) -> sspmv_status {
+        using V = decltype(tag);
+        grx_keys<V><<<gm, 256, 0, cu(s)>>>(m, n, A->row_offset, A->col_index, (const V *)A->values, sentinel, k_rc, k_cr,
+                                           v1, v2);
+        SSPMV_LAUNCH_CHECK();
+        return SSPMV_OK;
+    }));
+    const int kbits = bits_for(sentinel);
+    GTRY(radix_sort_pairs(k_rc, v1, nnz, kbits, s));
+    GTRY(radix_sort_pairs(k_cr, v2, nnz, kbits, s));
+    const uint64_t gpr = (uint64_t)((R + X - 1) / X), gpc = (uint64_t)((Cd + X - 1) / X);
+    if (do_c) {  // groups along columns: row-major keys, tiles of Cd columns
+        grx_runs<<<gz, 256, 0, cu(s)>>>(nnz, k_rc, sentinel, (uint64_t)n, (uint64_t)Cd, X, cnt + 1);
+        note_launch();
+    }
+    if (do_r) {
+        grx_runs<<<gz, 256, 0, cu(s)>>>(nnz, k_cr, sentinel, (uint64_t)m, (uint64_t)R, X, cnt + 0);
+        note_launch();
+        const uint64_t ps = (uint64_t)mb * gpr * (uint64_t)nb;
+        grx_pot_keys<<<gz, 256, 0, cu(s)>>>(nnz, k_rc, sentinel, (uint64_t)n, (uint64_t)R, (uint64_t)Cd, (uint64_t)X,
+                                            gpr, (uint64_t)nb, ps, k_pot);
+        note_launch();
+        GTRY(radix_sort_pairs(k_pot, v3, nnz, bits_for(ps), s));
+        count_distinct<<<gz, 256, 0, cu(s)>>>(nnz, k_pot, ps, cnt + 2);
+        note_launch();
+    }
+    if (do_c) {
+        const uint64_t ps = (uint64_t)nb * gpc * (uint64_t)mb;
+        grx_pot_keys<<<gz, 256, 0, cu(s)>>>(nnz, k_cr, sentinel, (uint64_t)m, (uint64_t)Cd, (uint64_t)R, (uint64_t)X,
+                                            gpc, (uint64_t)mb, ps, k_pot);
+        note_launch();
+        GTRY(radix_sort_pairs(k_pot, v3, nnz, bits_for(ps), s));
+        count_distinct<<<gz, 256, 0, cu(s)>>>(nnz, k_pot, ps, cnt + 3);
+        note_launch();
+    }
+    unsigned long long h[4] = {0, 0, 0, 0};
+    cudaError_t e = cudaMemcpyAsync(h, cnt, 32, cudaMemcpyDeviceToHost, cu(s));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cu(s));
+    release();
+#undef GTRY
+    if (e != cudaSuccess) return fail(SSPMV_CUDA_ERROR, "grx features: %s", cudaGetErrorString(e));
+    if (do_r) {
+        out[0] = (double)h[0] / (double)nnz;
+        out[2] = (double)h[2] / (double)((uint64_t)mb * gpr);
+    }
+    if (do_c) {
+        out[1] = (double)h[1] / (double)nnz;
+        out[3] = (double)h[3] / (double)((uint64_t)nb * gpc);
+    }
+    return SSPMV_OK;
+}
+
 static const char *kFeatureNames[SSPMV_NUM_FEATURES] = {
     "num_rows", "num_cols", "num_nnz", "nnz_ratio", "nnz_on_maindiag_ratio", "nnz_row_distance_ratio",
     "nz_row_ratio", "max_nnz_each_row", "ave_nnz_each_row", "standard_dev_row", "P-ratio_row", "Gini_coeff_row",

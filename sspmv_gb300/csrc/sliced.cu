@@ -307,20 +307,45 @@ __global__ void copy_u32_to_i32(int64_t n, const uint32_t *__restrict__ in, int3
         out[i] = (int32_t)in[i];
 }
 
-// chunk width = max row length in the chunk, rounded up to `align`
-__global__ void chunk_widths(int64_t m, int32_t C, int32_t align, int64_t nchunks, const int32_t *__restrict__ rp,
-                             const int32_t *__restrict__ reorder, int32_t *__restrict__ width,
+// chunk width = max row length in the chunk, rounded up to `align`.  Pass 1
+// (thread per stored row position) folds row lengths into width[] with
+// atomicMax -- one atomic per block when the block's rows lie in one chunk
+// (ELL is a single chunk of all rows), one per row otherwise; width[] starts
+// at zero.  Pass 2 rounds and sizes each chunk.
+__global__ void chunk_row_max(int64_t m, int32_t C, const int32_t *__restrict__ rp,
+                              const int32_t *__restrict__ reorder, int32_t *__restrict__ width) {
+    __shared__ int s_max[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = base + threadIdx.x;
+        int len = 0;
+        if (i < m) {
+            const int64_t r = reorder ? reorder[i] : i;
+            len = rp[r + 1] - rp[r];
+        }
+        const int64_t last = min(base + (int64_t)blockDim.x, m) - 1;
+        if (base / C == last / C) {  // block-uniform branch
+            int v = len;
+            for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+            if (lane == 0) s_max[warp] = v;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int b = 0;
+                for (int w = 0; w < nwarps; w++) b = max(b, s_max[w]);
+                if (b > 0) atomicMax(width + base / C, b);
+            }
+            __syncthreads();
+        } else if (len > 0) {
+            atomicMax(width + i / C, len);
+        }
+    }
+}
+
+__global__ void chunk_widths(int64_t nchunks, int32_t C, int32_t align, int32_t *__restrict__ width,
                              int64_t *__restrict__ slots) {
     for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < nchunks;
          c += (int64_t)gridDim.x * blockDim.x) {
-        int32_t w = 0;
-        for (int32_t q = 0; q < C; q++) {
-            const int64_t i = c * C + q;
-            if (i >= m) break;
-            const int64_t r = reorder ? reorder[i] : i;
-            w = max(w, rp[r + 1] - rp[r]);
-        }
-        w = ((w + align - 1) / align) * align;
+        const int32_t w = ((width[c] + align - 1) / align) * align;
         width[c] = w;
         slots[c] = (int64_t)w * C;
     }
@@ -397,10 +422,19 @@ sspmv_status build_sliced(const sspmv_csr *A, int32_t C, int32_t align, int64_t 
     st = dalloc(&b.width, (size_t)b.nchunks, s);
     if (st == SSPMV_OK) st = dalloc(&b.chunk_ptr, (size_t)b.nchunks + 1, s);
     if (st == SSPMV_OK && b.nchunks > 0) {
-        chunk_widths<<<grid_for(b.nchunks, 256, (int64_t)num_sms() * 16), 256, 0, cu(s)>>>(
-            m, C, align, b.nchunks, A->row_offset, b.reorder, b.width, b.chunk_ptr);
-        note_launch();
-        st = exclusive_scan_i64(b.chunk_ptr, b.chunk_ptr, b.nchunks, &b.total, s);
+        cudaError_t e = cudaMemsetAsync(b.width, 0, (size_t)b.nchunks * 4, cu(s));
+        if (e != cudaSuccess) st = fail(SSPMV_CUDA_ERROR, "width memset: %s", cudaGetErrorString(e));
+        if (st == SSPMV_OK && m > 0) {
+            chunk_row_max<<<grid_for(m, 256, (int64_t)num_sms() * 16), 256, 0, cu(s)>>>(m, C, A->row_offset,
+                                                                                      b.reorder, b.width);
+            note_launch();
+        }
+        if (st == SSPMV_OK) {
+            chunk_widths<<<grid_for(b.nchunks, 256, (int64_t)num_sms() * 16), 256, 0, cu(s)>>>(b.nchunks, C, align,
+                                                                                             b.width, b.chunk_ptr);
+            note_launch();
+            st = exclusive_scan_i64(b.chunk_ptr, b.chunk_ptr, b.nchunks, &b.total, s);
+        }
     }
     if (st == SSPMV_OK) {
         cudaError_t e = cudaMemcpyAsync(b.chunk_ptr + b.nchunks, &b.total, 8, cudaMemcpyHostToDevice, cu(s));
@@ -539,7 +573,7 @@ extern "C" sspmv_status sspmv_ell_export(const sspmv_ell *A, int32_t *col_index,
 
 extern "C" sspmv_status sspmv_delete_ell(sspmv_ell *A) {
     if (!A) return SSPMV_OK;
-    cudaDeviceSynchronize();
+    delete_barrier();
     free_plan(&A->f, nullptr);
     if (A->f.owns) {
         dfree(A->col_index, nullptr);
@@ -600,7 +634,7 @@ extern "C" sspmv_status sspmv_sell_export(const sspmv_s_ell *A, int32_t *row_wid
 
 extern "C" sspmv_status sspmv_delete_sell(sspmv_s_ell *A) {
     if (!A) return SSPMV_OK;
-    cudaDeviceSynchronize();
+    delete_barrier();
     free_plan(&A->f, nullptr);
     if (A->f.owns) {
         dfree(A->row_width, nullptr);
@@ -674,7 +708,7 @@ extern "C" sspmv_status sspmv_sell_c_sigma_export(const sspmv_sell_c_sigma *A, i
 
 extern "C" sspmv_status sspmv_delete_sell_c_sigma(sspmv_sell_c_sigma *A) {
     if (!A) return SSPMV_OK;
-    cudaDeviceSynchronize();
+    delete_barrier();
     free_plan(&A->f, nullptr);
     if (A->f.owns) {
         dfree(A->reorder, nullptr);
@@ -742,7 +776,7 @@ extern "C" sspmv_status sspmv_sell_c_R_export(const sspmv_sell_c_R *A, int32_t *
 
 extern "C" sspmv_status sspmv_delete_sell_c_R(sspmv_sell_c_R *A) {
     if (!A) return SSPMV_OK;
-    cudaDeviceSynchronize();
+    delete_barrier();
     free_plan(&A->f, nullptr);
     if (A->f.owns) {
         dfree(A->reorder, nullptr);

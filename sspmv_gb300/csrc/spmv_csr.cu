@@ -18,6 +18,7 @@
 #include "common.cuh"
 #include "plan.cuh"
 #include "spmv_common.cuh"
+#include "serve.cuh"
 
 namespace sspmv {
 namespace {
@@ -257,6 +258,124 @@ __global__ void csr_merge_fixup(int64_t num_tiles, int m, const int32_t *__restr
     for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
 }
 
+// ---------------------------------------------------- batched (serving) --
+// Index of the item owning global tile gt: the last item whose tile_begin is
+// <= gt (items of a group have increasing tile_begin).
+__device__ __forceinline__ int batch_item_of(const BatchItem *__restrict__ items, int n, int64_t gt) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&items[mid].tile_begin) <= gt) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Persistent merge-path kernel over the tiles of every request of group g:
+// CTA b takes global tiles b, b + gridDim.x, ...  The tile body is the one
+// the single-matrix kernel runs, with the request's own split points, and
+// the carries go to per-batch slots, so results match a lone sspmv_LeSpMV_csr
+// / sspmv_spmm_csr call bit for bit.
+template <typename V, int K>
+__global__ void __launch_bounds__(kBlock) csr_batch_kernel(int g, const BatchHeader *__restrict__ hdr,
+                                                           const BatchItem *__restrict__ all_items,
+                                                           int32_t *__restrict__ carry_row,
+                                                           int32_t *__restrict__ has_end, V *__restrict__ carry_val,
+                                                           V *__restrict__ head_val) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = hdr->n_items[g];
+    const int64_t total = hdr->total_tiles[g];
+    const int64_t base = hdr->carry_base[g];
+    const BatchItem *items = all_items + hdr->item_begin[g];
+    for (int64_t gt = blockIdx.x; gt < total; gt += gridDim.x) {
+        const BatchItem *q = items + batch_item_of(items, n, gt);
+        const int64_t t = gt - q->tile_begin;
+        const int2 *coords = q->coords;
+        merge_tile<V, K>(q->m, q->row_offset, q->col_index, (const V *)q->values, (const V *)q->x, q->ldx,
+                         (V)q->alpha, (V)q->beta, (V *)q->y, q->ldy, coords[t], coords[t + 1], base + gt,
+                         carry_row, has_end, carry_val, head_val, smem_raw);
+    }
+}
+
+// The batched counterpart of csr_merge_fixup: one thread per global tile.
+template <typename V, int K>
+__global__ void csr_batch_fixup(int g, const BatchHeader *__restrict__ hdr, const BatchItem *__restrict__ all_items,
+                                const int32_t *__restrict__ carry_row, const int32_t *__restrict__ has_end,
+                                const V *__restrict__ carry_val, const V *__restrict__ head_val) {
+    const int n = hdr->n_items[g];
+    const int64_t total = hdr->total_tiles[g];
+    const int64_t base = hdr->carry_base[g];
+    const BatchItem *items = all_items + hdr->item_begin[g];
+    for (int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gt < total;
+         gt += (int64_t)gridDim.x * blockDim.x) {
+        const BatchItem *q = items + batch_item_of(items, n, gt);
+        const int64_t t = gt - q->tile_begin, nt = q->num_tiles;
+        if (nt <= 1) continue;
+        const int64_t slot = base + gt;
+        const int r = carry_row[slot];
+        if (r >= q->m) continue;
+        const int rs = q->row_offset[r];
+        if (rs < q->coords[t].y || rs >= q->coords[t + 1].y) continue;
+        V tot[K];
+#pragma unroll
+        for (int c = 0; c < K; c++) tot[c] = carry_val[slot * kMaxK + c];
+        for (int64_t u = t + 1; u < nt; u++) {
+            const int64_t su = slot + (u - t);
+            if (has_end[su]) {
+#pragma unroll
+                for (int c = 0; c < K; c++) tot[c] += head_val[su * kMaxK + c];
+                break;
+            }
+#pragma unroll
+            for (int c = 0; c < K; c++) tot[c] += carry_val[su * kMaxK + c];
+        }
+        V *yp = (V *)q->y + (int64_t)r * q->ldy;
+        const V alpha = (V)q->alpha, beta = (V)q->beta;
+#pragma unroll
+        for (int c = 0; c < K; c++) yp[c] = axpby(alpha, tot[c], beta, yp + c);
+    }
+}
+
+template <typename V, int K>
+size_t merge_smem_bytes() {
+    return (size_t)MergeShape<K>::tile * K * sizeof(V) + ((size_t)MergeShape<K>::tile + 1) * 4;
+}
+
+// Resident CTAs per SM of csr_batch_kernel<V, K> (sets its shared-memory
+// attribute on first use).
+template <typename V, int K>
+int batch_blocks_per_sm() {
+    static int blocks = 0;
+    if (blocks == 0) {
+        const size_t smem = merge_smem_bytes<V, K>();
+        cudaFuncSetAttribute(csr_batch_kernel<V, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, csr_batch_kernel<V, K>, kBlock, smem) != cudaSuccess ||
+            b < 1)
+            b = 1;
+        blocks = b;
+    }
+    return blocks;
+}
+
+template <typename V, int K>
+sspmv_status launch_batch_vk(int g, const BatchHeader *hdr, const BatchItem *items, void *carry, int64_t slots,
+                             sspmv_stream_t s) {
+    unsigned char *c = (unsigned char *)carry;
+    int32_t *carry_row = (int32_t *)c;
+    int32_t *has_end = (int32_t *)(c + (size_t)slots * 4);
+    V *carry_val = (V *)(c + (size_t)slots * 8);
+    V *head_val = (V *)(c + (size_t)slots * (8 + kMaxK * 8));
+    const unsigned grid = (unsigned)(num_sms() * batch_blocks_per_sm<V, K>());
+    csr_batch_kernel<V, K><<<grid, kBlock, merge_smem_bytes<V, K>(), cu(s)>>>(g, hdr, items, carry_row, has_end,
+                                                                              carry_val, head_val);
+    SSPMV_LAUNCH_CHECK();
+    csr_batch_fixup<V, K><<<(unsigned)num_sms() * 2, 256, 0, cu(s)>>>(g, hdr, items, carry_row, has_end, carry_val,
+                                                                        head_val);
+    SSPMV_LAUNCH_CHECK();
+    return SSPMV_OK;
+}
+
 template <typename V, int K, int VS>
 __global__ void __launch_bounds__(kBlock) csr_vector_kernel(
     int m, const int32_t *__restrict__ row_offset, const int32_t *__restrict__ col_index,
@@ -422,6 +541,49 @@ sspmv_status ensure_merge_plan(Plan *p, int which, int64_t m, int64_t nnz, const
     SSPMV_LAUNCH_CHECK();
     mp = q;
     return SSPMV_OK;
+}
+
+int csr_merge_tile_items(int32_t k) { return k > 4 ? MergeShape<8>::tile : MergeShape<1>::tile; }
+
+sspmv_status csr_merge_coords(const sspmv_csr *A, int32_t k, const int2 **coords, int64_t *num_tiles,
+                              sspmv_stream_t s) {
+    Plan *p = get_plan(&A->f);
+    if (!p) return fail(SSPMV_OUT_OF_MEMORY, "plan allocation failed");
+    const int which = k > 4 ? 1 : 0;
+    SSPMV_TRY(ensure_merge_plan(p, which, A->f.num_rows, A->f.num_nnzs, A->row_offset, A->f.value_type, s));
+    *coords = p->merge[which].coords;
+    *num_tiles = p->merge[which].num_tiles;
+    return SSPMV_OK;
+}
+
+unsigned csr_batch_grid(int g) {
+    int b = 1;
+    switch (g) {
+    case 0: b = batch_blocks_per_sm<float, 1>(); break;
+    case 1: b = batch_blocks_per_sm<float, 2>(); break;
+    case 2: b = batch_blocks_per_sm<float, 4>(); break;
+    case 3: b = batch_blocks_per_sm<float, 8>(); break;
+    case 4: b = batch_blocks_per_sm<double, 1>(); break;
+    case 5: b = batch_blocks_per_sm<double, 2>(); break;
+    case 6: b = batch_blocks_per_sm<double, 4>(); break;
+    default: b = batch_blocks_per_sm<double, 8>(); break;
+    }
+    return (unsigned)(num_sms() * b);
+}
+
+sspmv_status launch_csr_batch_group(int g, const BatchHeader *d_hdr, const BatchItem *d_items, void *carry,
+                                    int64_t carry_slots, sspmv_stream_t s) {
+    switch (g) {
+    case 0: return launch_batch_vk<float, 1>(g, d_hdr, d_items, carry, carry_slots, s);
+    case 1: return launch_batch_vk<float, 2>(g, d_hdr, d_items, carry, carry_slots, s);
+    case 2: return launch_batch_vk<float, 4>(g, d_hdr, d_items, carry, carry_slots, s);
+    case 3: return launch_batch_vk<float, 8>(g, d_hdr, d_items, carry, carry_slots, s);
+    case 4: return launch_batch_vk<double, 1>(g, d_hdr, d_items, carry, carry_slots, s);
+    case 5: return launch_batch_vk<double, 2>(g, d_hdr, d_items, carry, carry_slots, s);
+    case 6: return launch_batch_vk<double, 4>(g, d_hdr, d_items, carry, carry_slots, s);
+    case 7: return launch_batch_vk<double, 8>(g, d_hdr, d_items, carry, carry_slots, s);
+    }
+    return fail(SSPMV_INVALID_ARG, "batch group %d out of range", g);
 }
 
 }  // namespace sspmv

@@ -320,6 +320,18 @@ def features(csr: CSR_Matrix, tile_blocks: int = 256, arrays: bool = False, stre
     return F
 
 
+GRX_NAMES = ("GrX_uniqR", "GrX_uniqC", "GrX_potReuseR", "GrX_potReuseC")
+
+
+def grx_features(csr: CSR_Matrix, tile_blocks: int = 256, group: int = 0, stream=None) -> np.ndarray:
+    """GrX_uniqR, GrX_uniqC, GrX_potReuseR, GrX_potReuseC (tile group
+    analysis, src/sparse_features.cpp:884-1065); group 0 = 64 / sizeof(value)."""
+    out = np.zeros(4)
+    call("sspmv_csr_grx_features", csr.ref(), int(tile_blocks), int(group), out.ctypes.data_as(C.c_void_p),
+         _stream(stream))
+    return out
+
+
 def read_csr_matrix(path: str, precision: int = 64) -> HostCSR:
     """read_csr_matrix (utils/sparse_io.cpp:180-204) on the host."""
     vt = F64 if precision == 64 else F32

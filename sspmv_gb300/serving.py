@@ -1,0 +1,343 @@
+"""Request server over the C ABI (sspmv_server_*), and its serving workload.
+
+A `Server` keeps registered matrices resident in HBM in their serving format
+(least-recently-used eviction under a byte budget) and serves SpMV / SpMM
+requests y = alpha*A*X + beta*Y with continuous batching: requests that
+arrive while batches run on the GPU are gathered into the next batch, whose
+CSR requests (k in 1, 2, 4, 8) run in one persistent merge-path launch per
+(value type, k) group replayed from a CUDA graph.  mode="per_request" serves
+each request with its own sspmv_spmm_<fmt> launch instead (the comparison
+point).
+
+The reference has no serving layer (its benchmark programs run one matrix per
+process); the workload below is the serving configuration the library is
+measured on: 64 resident matrices mixed across the synthetic families with N
+log-uniform in [1e3, 1e6], requests SpMV or SpMM with k in {1, 2, 4, 8}, FP64
+or FP32, Poisson arrivals.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib, synth
+from ._lib import ServerConfig, ServerStats, call, lib
+from .synth import HostCSR
+
+FORMAT_IDS = {"csr": 0, "coo": 1, "ell": 2, "sell": 3, "sell_c_sigma": 4, "sell_c_R": 5, "dia": 6, "bsr": 7,
+              "csr5": 8}
+MODES = {"batched": 0, "per_request": 1}
+DEVICE_BUFFERS = 1
+
+REQUEST_DTYPE = np.dtype({"names": ["matrix_id", "k", "alpha", "beta", "x", "ldx", "y", "ldy", "flags", "reserved"],
+                          "formats": ["<i4", "<i4", "<f8", "<f8", "<u8", "<i8", "<u8", "<i8", "<i4", "<i4"],
+                          "offsets": [0, 4, 8, 16, 24, 32, 40, 48, 56, 60], "itemsize": 64})
+INFO_DTYPE = np.dtype({"names": ["status", "batch_size", "batch_id", "arrival_ns", "launch_ns", "done_ns"],
+                       "formats": ["<i4", "<i4", "<i8", "<i8", "<i8", "<i8"],
+                       "offsets": [0, 4, 8, 16, 24, 32], "itemsize": 40})
+assert REQUEST_DTYPE.itemsize == C.sizeof(_lib.Request) and INFO_DTYPE.itemsize == C.sizeof(_lib.RequestInfo)
+
+
+def _vt(dtype) -> int:
+    return _lib.F64 if np.dtype(dtype) == np.float64 else _lib.F32
+
+
+class Server:
+    """Owns one sspmv_server.  Registered host arrays are kept referenced
+    here for as long as the server lives (the server reads them on load)."""
+
+    def __init__(self, mode: str = "batched", max_batch_requests: int = 0, max_batch_tiles: int = 0,
+                 arena_bytes: int = 0, stage_limit_bytes: int = 0, hbm_budget_bytes: int = 0,
+                 num_inflight: int = 0, use_graphs: bool = True):
+        cfg = ServerConfig()
+        cfg.mode = MODES[mode]
+        cfg.max_batch_requests = max_batch_requests
+        cfg.max_batch_tiles = max_batch_tiles
+        cfg.arena_bytes = arena_bytes
+        cfg.stage_limit_bytes = stage_limit_bytes
+        cfg.hbm_budget_bytes = hbm_budget_bytes
+        cfg.num_inflight = num_inflight
+        cfg.use_graphs = 1 if use_graphs else 0
+        h = C.c_void_p()
+        call("sspmv_server_create", C.byref(cfg), C.byref(h))
+        self._h = h
+        self.mode = mode
+        self._keep: dict[int, HostCSR] = {}
+        self.shapes: dict[int, tuple[int, int, np.dtype]] = {}
+
+    def close(self) -> None:
+        if self._h:
+            call("sspmv_server_destroy", self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_matrix(self, mid: int, A: HostCSR, fmt: str = "csr", params=None) -> None:
+        A = HostCSR(A.num_rows, A.num_cols, np.ascontiguousarray(A.row_offset, np.int32),
+                    np.ascontiguousarray(A.col_index, np.int32), np.ascontiguousarray(A.values))
+        p = None
+        if params:
+            p = (C.c_int32 * 4)(*(list(params) + [0] * (4 - len(params))))
+        call("sspmv_server_add_matrix", self._h, int(mid), _vt(A.values.dtype), A.num_rows, A.num_cols, A.nnz,
+             A.row_offset.ctypes.data, A.col_index.ctypes.data if A.nnz else None,
+             A.values.ctypes.data if A.nnz else None, FORMAT_IDS[fmt], p)
+        self._keep[mid] = A
+        self.shapes[mid] = (A.num_rows, A.num_cols, A.values.dtype)
+
+    def preload(self, mid: int) -> None:
+        call("sspmv_server_preload", self._h, int(mid))
+
+    @staticmethod
+    def _ld(a, k: int) -> int:
+        if a.ndim == 1:
+            return k
+        return int(a.stride(0)) if callable(getattr(a, "stride", None)) else a.strides[0] // a.itemsize
+
+    @staticmethod
+    def _ptr(a) -> int:
+        if hasattr(a, "data_ptr"):
+            return int(a.data_ptr())
+        return int(a.ctypes.data)
+
+    def submit(self, mid: int, x, y, alpha: float = 1.0, beta: float = 0.0, k: int | None = None,
+               device: bool = False) -> int:
+        """x: num_cols x k (or num_cols) host array (device tensor with
+        device=True), y likewise num_rows x k; both must stay alive until
+        wait() returns."""
+        if k is None:
+            k = 1 if x.ndim == 1 else int(x.shape[1])
+        r = _lib.Request(int(mid), int(k), float(alpha), float(beta), self._ptr(x), self._ld(x, k), self._ptr(y),
+                         self._ld(y, k), DEVICE_BUFFERS if device else 0, 0)
+        t = C.c_int64()
+        call("sspmv_server_submit", self._h, C.byref(r), C.byref(t))
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = -1.0) -> dict:
+        info = _lib.RequestInfo()
+        st = lib.sspmv_server_wait(self._h, int(ticket), float(timeout), C.byref(info))
+        _lib.check(st, "sspmv_server_wait")
+        return {f: getattr(info, f) for f, _ in _lib.RequestInfo._fields_}
+
+    def replay(self, reqs: np.ndarray, arrival_ns: np.ndarray) -> np.ndarray:
+        """Open-loop load: request i is submitted arrival_ns[i] after the
+        call starts; returns one INFO_DTYPE record per request."""
+        reqs = np.ascontiguousarray(reqs, REQUEST_DTYPE)
+        arrival_ns = np.ascontiguousarray(arrival_ns, np.int64)
+        infos = np.zeros(len(reqs), INFO_DTYPE)
+        st = lib.sspmv_server_replay(self._h, len(reqs), reqs.ctypes.data, arrival_ns.ctypes.data,
+                                     infos.ctypes.data)
+        _lib.check(st, "sspmv_server_replay")
+        return infos
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        call("sspmv_server_get_stats", self._h, C.byref(s))
+        return {f: getattr(s, f) for f, _ in ServerStats._fields_}
+
+
+# --------------------------------------------------------------- workload --
+FAMILIES = ("banded", "powerlaw", "block", "uniform")
+
+
+def serving_matrix(family: str, n: int, seed: int) -> HostCSR:
+    """One matrix of the serving mix (FP64 values; FP32 copies are rounded)."""
+    if family == "banded":
+        p = synth.banded(n)
+    elif family == "powerlaw":
+        p = synth.powerlaw(n, 1.8, 16.0, min(50000, n))
+    elif family == "block":
+        p = synth.block(n, 4, max(1, n // 4))
+    else:
+        p = synth.uniform(n, min(32, n))
+    return synth.generate(p, seed, np.float64)
+
+
+def serving_matrices(num: int = 64, n_min: int = 1000, n_max: int = 1_000_000, seed: int = 0) -> list[dict]:
+    """`num` matrices cycling over the four families, N log-uniform in
+    [n_min, n_max] (seeded)."""
+    rng = np.random.default_rng(seed)
+    ns = np.exp(rng.uniform(np.log(n_min), np.log(n_max), num)).astype(np.int64)
+    out = []
+    for i in range(num):
+        fam = FAMILIES[i % len(FAMILIES)]
+        n = int(ns[i])
+        if fam == "block":
+            n = max(4, n - n % 4)
+        out.append({"family": fam, "n": n, "A": serving_matrix(fam, n, 100 + i)})
+    return out
+
+
+@dataclass
+class RequestStream:
+    reqs: np.ndarray        # REQUEST_DTYPE
+    arrival_ns: np.ndarray  # int64, ascending
+    matrix: np.ndarray      # served matrix index per request
+    k: np.ndarray
+    f64: np.ndarray
+
+
+def request_stream(num_requests: int, matrix_ids_f64: list[int], matrix_ids_f32: list[int], rate: float,
+                   seed: int = 1, ks=(1, 2, 4, 8)) -> RequestStream:
+    """Poisson arrivals at `rate` requests/s (rate <= 0: all at time 0);
+    each request picks a matrix uniformly, k uniformly from ks and FP64 or
+    FP32 with equal odds.  Buffers are filled in by the caller."""
+    rng = np.random.default_rng(seed)
+    nm = len(matrix_ids_f64)
+    mat = rng.integers(0, nm, num_requests)
+    k = np.asarray(ks)[rng.integers(0, len(ks), num_requests)]
+    f64 = rng.integers(0, 2, num_requests).astype(bool)
+    if rate > 0:
+        gaps = rng.exponential(1.0 / rate, num_requests)
+        arrival = np.cumsum(gaps) * 1e9
+        arrival -= arrival[0]
+    else:
+        arrival = np.zeros(num_requests)
+    reqs = np.zeros(num_requests, REQUEST_DTYPE)
+    ids64, ids32 = np.asarray(matrix_ids_f64), np.asarray(matrix_ids_f32)
+    reqs["matrix_id"] = np.where(f64, ids64[mat], ids32[mat])
+    reqs["k"] = k
+    reqs["alpha"] = 1.0
+    reqs["beta"] = 0.0
+    reqs["ldx"] = k
+    reqs["ldy"] = k
+    return RequestStream(reqs, arrival.astype(np.int64), mat, k, f64)
+
+
+def latency_summary(infos: np.ndarray) -> dict:
+    """p50 / p99 latency (arrival to result in the caller's buffer) and the
+    completed-requests throughput of one replay."""
+    ok = infos["status"] == 0
+    lat = (infos["done_ns"] - infos["arrival_ns"])[ok] / 1e3
+    span = (infos["done_ns"].max() - infos["arrival_ns"].min()) / 1e9 if len(infos) else 0.0
+    bs = infos["batch_size"][ok]
+    return {"requests": int(len(infos)), "failed": int((~ok).sum()),
+            "req_per_s": float(ok.sum() / span) if span > 0 else 0.0,
+            "p50_us": float(np.percentile(lat, 50)) if len(lat) else None,
+            "p99_us": float(np.percentile(lat, 99)) if len(lat) else None,
+            "mean_batch": float(bs.mean()) if len(bs) else 0.0}
+
+
+# -------------------------------------------------------------- benchmark --
+class ServingBench:
+    """The serving workload on one GPU: `num_matrices` matrices registered in
+    FP64 (ids 2i) and FP32 (ids 2i+1), one X and one Y buffer per id holding
+    up to 8 right-hand sides (pinned host memory, or device memory with
+    device_buffers=True).  Requests on one id share its buffers, so
+    overlapping requests write the same Y: the benchmark times the serving
+    path, the parity tests check results."""
+
+    def __init__(self, num_matrices: int = 64, seed: int = 0, device_buffers: bool = False, log=None):
+        import torch
+        self.log = log or (lambda *a: None)
+        self.mats = serving_matrices(num_matrices, seed=seed)
+        self.device_buffers = device_buffers
+        self.host = {}
+        self.xbuf, self.ybuf = {}, {}
+        for i, d in enumerate(self.mats):
+            A64 = d["A"]
+            for mid, A in ((2 * i, A64), (2 * i + 1, A64.astype(np.float32))):
+                self.host[mid] = A
+                tdt = torch.float64 if A.values.dtype == np.float64 else torch.float32
+                if device_buffers:
+                    x = torch.rand(A.num_cols * 8, dtype=tdt, device="cuda") * 2 - 1
+                    y = torch.zeros(A.num_rows * 8, dtype=tdt, device="cuda")
+                else:
+                    x = torch.empty(A.num_cols * 8, dtype=tdt, pin_memory=True)
+                    x.copy_(torch.from_numpy(synth.vector(A.num_cols * 8, mid, A.values.dtype)))
+                    y = torch.zeros(A.num_rows * 8, dtype=tdt, pin_memory=True)
+                self.xbuf[mid], self.ybuf[mid] = x, y
+        self.ids64 = [2 * i for i in range(len(self.mats))]
+        self.ids32 = [2 * i + 1 for i in range(len(self.mats))]
+        self.total_nnz = sum(d["A"].nnz for d in self.mats)
+
+    def server(self, mode: str, fmt_of=None, **kw) -> Server:
+        s = Server(mode=mode, **kw)
+        for mid, A in self.host.items():
+            fmt, params = fmt_of(mid, A) if fmt_of else ("csr", None)
+            s.add_matrix(mid, A, fmt, params)
+        for mid in self.host:
+            s.preload(mid)
+        return s
+
+    def stream(self, num_requests: int, rate: float, seed: int) -> RequestStream:
+        rs = request_stream(num_requests, self.ids64, self.ids32, rate, seed)
+        mids = rs.reqs["matrix_id"]
+        rs.reqs["x"] = [self.xbuf[m].data_ptr() for m in mids]
+        rs.reqs["y"] = [self.ybuf[m].data_ptr() for m in mids]
+        rs.reqs["flags"] = DEVICE_BUFFERS if self.device_buffers else 0
+        return rs
+
+    def run(self, s: Server, num_requests: int, rate: float, seed: int) -> dict:
+        rs = self.stream(num_requests, rate, seed)
+        infos = s.replay(rs.reqs, rs.arrival_ns)
+        out = latency_summary(infos)
+        out["offered_per_s"] = float(rate) if rate > 0 else None
+        return out
+
+
+def serving_benchmark(num_matrices: int = 64, device_buffers: bool = False, duration_s: float = 1.5,
+                      seed: int = 0, log=None) -> dict:
+    """Saturation throughput of the batched server and of per-request CSR
+    launches, then p50/p99 under Poisson load swept up to saturation.
+    'Equal p99' compares throughput at the per-request server's p99 at 70% of
+    its saturation rate."""
+    log = log or (lambda *a: None)
+    b = ServingBench(num_matrices, seed, device_buffers, log)
+    res = {"matrices": num_matrices, "registered": 2 * num_matrices, "total_nnz_per_precision": b.total_nnz,
+           "buffers": "device" if device_buffers else "pinned host", "modes": {},
+           "server_config": {"per_request": {"num_inflight": 8, "arena_bytes": 160 << 20},
+                             "batched": {"num_inflight": 3, "arena_bytes": 512 << 20}}}
+    # Per-request launches get more requests in flight (they cannot batch).
+    server_kw = res["server_config"]
+    for mode in ("per_request", "batched"):
+        s = b.server(mode, **server_kw[mode])
+        try:
+            b.run(s, 2000, 0.0, seed + 1)  # warm: graphs for the group sets, pools
+            sat = b.run(s, 20000 if mode == "batched" else 8000, 0.0, seed + 2)
+            log(f"[serving] {mode}: saturation {sat['req_per_s']:.0f} req/s, mean batch {sat['mean_batch']:.1f}")
+            res["modes"][mode] = {"saturation": sat, "sweep": [], "stats": None}
+            res["modes"][mode]["_server"] = s
+        except Exception:
+            s.close()
+            raise
+    base = res["modes"]["per_request"]["saturation"]["req_per_s"]
+    fracs = {"per_request": (0.3, 0.5, 0.7, 0.9), "batched": (0.3, 0.7, 1.0, 1.5, 2.0, 3.0, 4.0, 6.0, 8.0)}
+    try:
+        for mode in ("per_request", "batched"):
+            m = res["modes"][mode]
+            satm = m["saturation"]["req_per_s"]
+            for f in fracs[mode]:
+                rate = f * base
+                if rate > 1.05 * satm:
+                    break
+                n = int(min(max(rate * duration_s, 1000), 200000))
+                r = b.run(m["_server"], n, rate, seed + 10 + int(f * 100))
+                r["fraction_of_per_request_saturation"] = f
+                m["sweep"].append(r)
+                log(f"[serving] {mode} @ {rate:.0f}/s: {r['req_per_s']:.0f} req/s p50 {r['p50_us']:.0f} us "
+                    f"p99 {r['p99_us']:.0f} us batch {r['mean_batch']:.1f}")
+            m["stats"] = m["_server"].stats()
+    finally:
+        for mode in res["modes"].values():
+            mode.pop("_server").close()
+    pr = [r for r in res["modes"]["per_request"]["sweep"] if r["fraction_of_per_request_saturation"] == 0.7]
+    if pr:
+        target = pr[0]["p99_us"]
+        ok = [r for r in res["modes"]["batched"]["sweep"] if r["p99_us"] is not None and r["p99_us"] <= target]
+        best = max((r["req_per_s"] for r in ok), default=None)
+        res["equal_p99"] = {"p99_target_us": target, "per_request_req_per_s": pr[0]["req_per_s"],
+                            "batched_req_per_s": best,
+                            "throughput_ratio": (best / pr[0]["req_per_s"]) if best else None}
+    return res

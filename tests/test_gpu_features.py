@@ -39,3 +39,19 @@ def test_gpu_features_families(fam, T, oracle_lib):
     assert not bad, f"features differ (index, gpu, oracle): {bad[:5]}"
     for k in ao:
         assert np.array_equal(arrs[k], ao[k]), k
+
+
+@pytest.mark.parametrize("T,X", [(256, 8), (64, 4), (2048, 4), (16, 8)])
+@pytest.mark.parametrize("fam", ["powerlaw", "banded", "block", "wide", "zeros"])
+def test_gpu_grx_features_match_oracle(fam, T, X, oracle_lib):
+    from sspmv_gb300 import lespmv as L
+    from sspmv_gb300 import synth
+    p = {"powerlaw": synth.powerlaw(6000, 1.8, 16.0, 3000, 0.05), "banded": synth.banded(8000, (0, 1, -1, 2, 5, -9)),
+         "block": synth.block(6000, 4, 1500), "wide": synth.uniform(3000, 10, 0.1, num_cols=9000),
+         "zeros": synth.block(4000, 8, 300)}[fam]
+    A = synth.generate(p, 5)
+    if fam == "zeros":
+        A.values[::7] = 0.0  # explicit zeros are absent entries
+    g = L.grx_features(L.csr_from_host(A), T, X)
+    o = oracle_lib.grx(A, T, X)
+    assert np.array_equal(g, o), f"gpu {g} oracle {o}"
