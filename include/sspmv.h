@@ -230,7 +230,9 @@ sspmv_status sspmv_delete_csr(sspmv_csr *A);
 
 /* ---------------- SpMV / SpMM ---------------- */
 /* LeSpMV_csr (src/spmv_csr.cpp:165-185).  kernel_flag 0/2: nnz-balanced
- * merge-path kernel; 1: vector-per-row kernel. */
+ * merge-path kernel; 1: vector-per-row kernel; 3: nonzero-split stream
+ * kernel (256 nonzeros per warp; matrices with runs of more than 256 empty
+ * rows use merge-path). */
 sspmv_status sspmv_LeSpMV_csr(double alpha, const sspmv_csr *A, const void *x, double beta, void *y,
                               sspmv_stream_t stream);
 sspmv_status sspmv_spmm_csr(double alpha, const sspmv_csr *A, int32_t k, const void *X, int64_t ldx,
@@ -504,7 +506,7 @@ sspmv_status sspmv_nn_adam(int64_t n, float *w, const float *g, float *m, float 
  * with leading dimensions, HOST buffers) with continuous batching: while
  * batches are on the GPU, the requests that arrive are gathered into the
  * next one.  CSR requests with k in {1, 2, 4, 8} of a batch run in one
- * persistent merge-path launch per (value type, k) group, replayed from a
+ * persistent stream-kernel launch per (value type, k) group, replayed from a
  * CUDA graph; other requests get their format's own launch in the same
  * batch.  A request's result is bit-identical whatever else is batched with
  * it.  Mode SSPMV_SERVE_PER_REQUEST serves one request at a time through
@@ -526,7 +528,7 @@ typedef enum { SSPMV_SERVE_BATCHED = 0, SSPMV_SERVE_PER_REQUEST = 1 } sspmv_serv
 typedef struct {
     int32_t mode;               /* sspmv_serve_mode */
     int32_t max_batch_requests; /* 0: 1024 */
-    int64_t max_batch_tiles;    /* merge tiles (carry slots) per batch; 0: 1 << 17 */
+    int64_t max_batch_tiles;    /* 256-nonzero chunks (carry slots) per batch; 0: 1 << 20 */
     int64_t arena_bytes;        /* per batch in flight, device staging for X and for Y each; 0: 512 MiB */
     int64_t stage_limit_bytes;  /* X / Y up to this size are packed through pinned staging; 0: 1 MiB */
     int64_t hbm_budget_bytes;   /* resident matrices; 0: 120e9 */

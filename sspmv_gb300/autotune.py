@@ -6,7 +6,7 @@ on the GPU, timed with CUDA events with L2 flushed before every run, and the
 fastest is kept.  Results are plain dicts, so a caller can store them as an
 append-only JSONL log keyed by matrix and re-apply them without re-measuring.
 
-CSR candidates: merge-path kernel, vector kernel with 2..32 lanes per row.
+CSR candidates: stream kernel (default), merge-path kernel, vector kernel with 2..32 lanes per row.
 SELL-c-sigma candidates (re-conversion per point): C in {8,16,32} x sigma in
 {256, 4096, N}.  BSR candidates: r x c in {2,4,8,16}^2 (feasible ones).
 """
@@ -40,7 +40,7 @@ def time_spmv(M, x, y, reps: int = 10, warmup: int = 2, flush=None, stream=None)
     return ts[len(ts) // 2]
 
 
-CSR_CANDIDATES = [(0, 0)] + [(1, vs) for vs in (2, 4, 8, 16, 32)]
+CSR_CANDIDATES = [(0, 0), (2, 0)] + [(1, vs) for vs in (2, 4, 8, 16, 32)]
 
 
 def tune_kernel(M, x, y, candidates, reps: int = 10) -> dict:

@@ -267,110 +267,173 @@ __global__ void __launch_bounds__(kBlock) coo_tile_kernel(
     }
 }
 
-// Warp kernel (default): a warp takes kWarpChunk consecutive nonzeros in
-// steps of 32, runs a segmented shuffle scan keyed by row over each step and
-// carries the open row into the next step.  A lane whose nonzero is the last
-// of its row writes that row -- unless the row began before the warp's chunk
-// (head piece) -- and the chunk's open last row is left as a carry.  No
-// shared memory, no barriers.  The loads of kBatch steps (row, column, value,
-// then the x gathers) are issued before any of them is scanned, so each lane
-// keeps kBatch independent gathers in flight.
-constexpr int kWarpChunk = 256;
+// Warp kernel (default): a warp takes kWarpChunk = 256 consecutive nonzeros,
+// lane l the 8 consecutive ones at 8l (vector loads of rows, columns and
+// values; all 8 gathers of x issued before use for k <= 2).  Each lane sums
+// its nonzeros in order, writing every row that starts and ends inside its 8;
+// the open sum before its first row end (head) and after its last (tail) are
+// joined across lanes by one segmented shuffle scan keyed by "lane has a row
+// end".  The row that ends first in a lane gets head + the carried tail sum;
+// a row that began before the warp's chunk is left in head_val for the
+// fix-up, and the chunk's open last row in carry_val.  No shared memory, no
+// barriers, one shuffle scan per 256 nonzeros.
+constexpr int kCooPerLane = 8;
+constexpr int kWarpChunk = 32 * kCooPerLane;
+
+template <typename V>
+struct Vec2 {
+    using T = double2;
+};
+template <>
+struct Vec2<float> {
+    using T = float4;
+};
+
+// Loads this lane's 8 consecutive nonzeros (n_valid of them exist).
+template <typename V>
+__device__ __forceinline__ void coo_load8(const int32_t *__restrict__ ri, const int32_t *__restrict__ ci,
+                                          const V *__restrict__ cv, int64_t e0, int nv, bool vec, int (&r)[8],
+                                          int (&c)[8], V (&a)[8]) {
+    if (vec && nv == 8) {
+        const int4 r0 = __ldcs(reinterpret_cast<const int4 *>(ri + e0));
+        const int4 r1 = __ldcs(reinterpret_cast<const int4 *>(ri + e0 + 4));
+        const int4 c0 = __ldcs(reinterpret_cast<const int4 *>(ci + e0));
+        const int4 c1 = __ldcs(reinterpret_cast<const int4 *>(ci + e0 + 4));
+        r[0] = r0.x; r[1] = r0.y; r[2] = r0.z; r[3] = r0.w; r[4] = r1.x; r[5] = r1.y; r[6] = r1.z; r[7] = r1.w;
+        c[0] = c0.x; c[1] = c0.y; c[2] = c0.z; c[3] = c0.w; c[4] = c1.x; c[5] = c1.y; c[6] = c1.z; c[7] = c1.w;
+        if constexpr (sizeof(V) == 8) {
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const double2 v = __ldcs(reinterpret_cast<const double2 *>(cv + e0) + h);
+                a[2 * h] = v.x;
+                a[2 * h + 1] = v.y;
+            }
+        } else {
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const float4 v = __ldcs(reinterpret_cast<const float4 *>(cv + e0) + h);
+                a[4 * h] = v.x; a[4 * h + 1] = v.y; a[4 * h + 2] = v.z; a[4 * h + 3] = v.w;
+            }
+        }
+        return;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+        r[u] = u < nv ? ld_stream(ri + e0 + u) : -1;
+        c[u] = u < nv ? ld_stream(ci + e0 + u) : 0;
+        a[u] = u < nv ? ld_stream(cv + e0 + u) : V(0);
+    }
+}
 
 template <typename V, int K>
 __global__ void __launch_bounds__(kBlock) coo_warp_kernel(
     int64_t nnz, const int32_t *__restrict__ ri, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
     int32_t *__restrict__ carry_row, int32_t *__restrict__ has_end, V *__restrict__ carry_val,
-    V *__restrict__ head_val) {
-    constexpr int kSteps = kWarpChunk / 32;
-    constexpr int kBatch = K <= 2 ? kSteps : K <= 4 ? 4 : 2;
+    V *__restrict__ head_val, int vec) {
+    constexpr unsigned kFull = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t j0 = w * kWarpChunk;
-    if (j0 >= nnz) return;
+    if (j0 >= nnz) return;  // warp-uniform
     const int64_t j1 = min(j0 + (int64_t)kWarpChunk, nnz);
-    const int first_row = __ldg(ri + j0);
+    const int64_t e0 = j0 + (int64_t)lane * kCooPerLane;
+    const int nv = (int)max((int64_t)0, min((int64_t)kCooPerLane, j1 - e0));
+    int r[8], c[8];
+    V a[8];
+    coo_load8<V>(ri, ci, cv, e0, nv, vec != 0, r, c, a);
+    const int first_row = __shfl_sync(kFull, r[0], 0);
     const bool head_open = j0 > 0 && __ldg(ri + j0 - 1) == first_row;  // chunk starts inside a row
-    int carry_r = -1;
-    V carry[K];
+    // row of the nonzero after this lane's last one
+    int next = __shfl_down_sync(kFull, r[0], 1);
+    if (nv > 0 && e0 + nv == j1) next = j1 < nnz ? __ldg(ri + j1) : -1;
+    V xv[K <= 2 ? 8 : 1][K];
+    if constexpr (K <= 2) {
 #pragma unroll
-    for (int q = 0; q < K; q++) carry[q] = V(0);
-    bool first_ended = false;
-    for (int s0 = 0; s0 < kSteps; s0 += kBatch) {
-        if (j0 + (int64_t)s0 * 32 >= j1) break;
-        int rr[kBatch], cc[kBatch];
-        V aa[kBatch];
+        for (int u = 0; u < 8; u++)
 #pragma unroll
-        for (int u = 0; u < kBatch; u++) {
-            const int64_t e = j0 + (int64_t)(s0 + u) * 32 + lane;
-            rr[u] = -1 - lane;  // unique keys for idle lanes
-            cc[u] = -1;
-            aa[u] = V(0);
-            if (e < j1) {
-                rr[u] = ld_stream(ri + e);
-                cc[u] = ld_stream(ci + e);
-                aa[u] = ld_stream(cv + e);
+            for (int q = 0; q < K; q++) xv[u][q] = u < nv ? ld_x(x + (int64_t)c[u] * ldx + q) : V(0);
+    }
+    V seg[K], head[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) seg[q] = head[q] = V(0);
+    bool any_end = false;
+    int head_row = -1, last_row = -1;
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+        if (u < nv) {
+            last_row = r[u];
+#pragma unroll
+            for (int q = 0; q < K; q++) {
+                if constexpr (K <= 2) seg[q] += a[u] * xv[u][q];
+                else seg[q] += a[u] * ld_x(x + (int64_t)c[u] * ldx + q);
             }
-        }
-        V pp[kBatch][K];
+            const int rn = u + 1 < nv ? r[u + 1] : next;
+            if (rn != r[u]) {  // r[u] ends here
+                if (!any_end) {
+                    any_end = true;
+                    head_row = r[u];
 #pragma unroll
-        for (int u = 0; u < kBatch; u++)
-#pragma unroll
-            for (int q = 0; q < K; q++) pp[u][q] = cc[u] >= 0 ? aa[u] * ld_x(x + (int64_t)cc[u] * ldx + q) : V(0);
-#pragma unroll
-        for (int u = 0; u < kBatch; u++) {
-            const int64_t base = j0 + (int64_t)(s0 + u) * 32;
-            if (base >= j1) break;
-            const int64_t e = base + lane;
-            const bool valid = e < j1;
-            const int r = rr[u];
-            V *p = pp[u];
-            if (lane == 0 && r == carry_r) {
-#pragma unroll
-                for (int q = 0; q < K; q++) p[q] += carry[q];
-            }
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int r2 = __shfl_up_sync(0xffffffffu, r, o);
-                V v2[K];
-#pragma unroll
-                for (int q = 0; q < K; q++) v2[q] = __shfl_up_sync(0xffffffffu, p[q], o);
-                if (lane >= o && r2 == r) {
-#pragma unroll
-                    for (int q = 0; q < K; q++) p[q] += v2[q];
-                }
-            }
-            // row of the next nonzero in the matrix
-            int rn = __shfl_down_sync(0xffffffffu, r, 1);
-            if (valid && (lane == 31 || e + 1 >= j1)) rn = e + 1 < nnz ? __ldg(ri + e + 1) : -1;
-            const bool ends = valid && rn != r;
-            if (ends) {
-                if (r == first_row && head_open) {
-                    V *hp = head_val + w * kMaxK;
-#pragma unroll
-                    for (int q = 0; q < K; q++) hp[q] = p[q];
+                    for (int q = 0; q < K; q++) head[q] = seg[q];
                 } else {
-                    V *yp = y + (int64_t)r * ldy;
+                    V *yp = y + (int64_t)r[u] * ldy;
 #pragma unroll
-                    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, p[q], beta, yp + q);
+                    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, seg[q], beta, yp + q);
                 }
-            }
-            if (__any_sync(0xffffffffu, ends && r == first_row)) first_ended = true;
-            // open row at the end of this step -> next step / next chunk
-            const int last = (int)min((int64_t)31, j1 - 1 - base);
-            carry_r = __shfl_sync(0xffffffffu, ends ? -2 : r, last);
 #pragma unroll
-            for (int q = 0; q < K; q++) carry[q] = __shfl_sync(0xffffffffu, p[q], last);
+                for (int q = 0; q < K; q++) seg[q] = V(0);
+            }
         }
     }
-    if (lane == 0) {
-        has_end[w] = first_ended ? 1 : 0;
-        carry_row[w] = carry_r >= 0 ? carry_r : -1;
-        if (carry_r >= 0) {
+    // segmented inclusive scan of the open tails; a lane with a row end starts a segment
+    V S[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) S[q] = seg[q];
+    bool f = any_end;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        V up[K];
+#pragma unroll
+        for (int q = 0; q < K; q++) up[q] = __shfl_up_sync(kFull, S[q], o);
+        const bool fu = __shfl_up_sync(kFull, f, o);
+        if (lane >= o) {
+            if (!f) {
+#pragma unroll
+                for (int q = 0; q < K; q++) S[q] += up[q];
+            }
+            f = f || fu;
+        }
+    }
+    V cin[K];  // tail sums carried into this lane's first row
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        cin[q] = __shfl_up_sync(kFull, S[q], 1);
+        if (lane == 0) cin[q] = V(0);
+    }
+    if (any_end) {
+        V tot[K];
+#pragma unroll
+        for (int q = 0; q < K; q++) tot[q] = head[q] + cin[q];
+        if (head_row == first_row && head_open) {
+            V *hp = head_val + w * kMaxK;
+#pragma unroll
+            for (int q = 0; q < K; q++) hp[q] = tot[q];
+        } else {
+            V *yp = y + (int64_t)head_row * ldy;
+#pragma unroll
+            for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
+        }
+    }
+    const bool chunk_end = __any_sync(kFull, any_end);
+    // the lane holding the chunk's last nonzero reports the open last row
+    if (nv > 0 && e0 + nv == j1) {
+        const bool open = next == last_row;
+        has_end[w] = chunk_end ? 1 : 0;
+        carry_row[w] = open ? last_row : -1;
+        if (open) {
             V *cp = carry_val + w * kMaxK;
 #pragma unroll
-            for (int q = 0; q < K; q++) cp[q] = carry[q];
+            for (int q = 0; q < K; q++) cp[q] = S[q];
         }
     }
 }
@@ -487,9 +550,11 @@ sspmv_status coo_pass(const sspmv_coo *A, Plan *p, V alpha, const V *x, int64_t 
     }
     if (nnz == 0) return SSPMV_OK;
     if (warp_kernel) {
+        const int vec = ((reinterpret_cast<uintptr_t>(A->row_index) | reinterpret_cast<uintptr_t>(A->col_index) |
+                          reinterpret_cast<uintptr_t>(A->values)) & 15) == 0;
         coo_warp_kernel<V, K><<<grid_for(nt * 32, kBlock), kBlock, 0, cu(s)>>>(
             nnz, A->row_index, A->col_index, (const V *)A->values, x, ldx, alpha, beta, y, ldy, ints, ints + nt,
-            (V *)p->extra[which * 3 + 1], (V *)p->extra[which * 3 + 2]);
+            (V *)p->extra[which * 3 + 1], (V *)p->extra[which * 3 + 2], vec);
         SSPMV_LAUNCH_CHECK();
         if (nt > 1) {
             coo_fixup<V, K><<<grid_for(nt, 256), 256, 0, cu(s)>>>(nt, A->row_index, tile, ints, ints + nt,

@@ -3,13 +3,13 @@
 //
 // Threads.  Callers submit requests into a FIFO queue.  One worker thread
 // forms batches: it takes queued requests in order while the batch still has
-// room (requests, merge tiles, staging bytes), loading matrices that are not
+// room (requests, nonzero chunks, staging bytes), loading matrices that are not
 // resident (and evicting idle ones, least recently used first), then issues
 // the batch on the stream of a free workspace -- one H2D copy of the packed
-// descriptors and small vectors, the batched CSR launches (a CUDA graph per
-// set of (value type, k) groups present), per-request launches for the other
-// formats, one D2H copy of the packed small results -- and hands it to the
-// completion thread.  With `num_inflight` workspaces, the next batch is formed
+// descriptors and small vectors, the batched CSR launches (persistent stream
+// kernels of every (value type, k) group, one CUDA graph per workspace),
+// per-request launches for the other formats, one D2H copy of the packed
+// small results -- and hands it to the completion thread.  With `num_inflight` workspaces, the next batch is formed
 // and issued while earlier ones run, so requests that arrive while the GPU is
 // busy join the next batch as soon as a workspace is free.  The completion
 // thread waits for each batch in issue order, copies packed results into the
@@ -73,8 +73,9 @@ struct Matrix {
     int64_t bytes = 0;
     int64_t refs = 0;        // requests in batches not yet completed (or being formed)
     uint64_t last_use = 0;   // LRU clock
-    const int2 *coords[2] = {nullptr, nullptr};  // CSR merge split points, k <= 4 and k == 8
-    int64_t tiles[2] = {0, 0};
+    const int32_t *row_start = nullptr;  // CSR stream plan: first row of each 256-nonzero chunk
+    int64_t chunks = 0;
+    bool batchable = false;              // the batched stream kernel takes this matrix
     // The plan of a matrix (carry buffers) is shared by its per-request
     // launches: launches on different streams are ordered through this event.
     cudaEvent_t ev = nullptr;
@@ -102,7 +103,7 @@ struct Workspace {
     cudaEvent_t done = nullptr;
     unsigned char *h_in = nullptr, *d_in = nullptr, *h_out = nullptr, *d_out = nullptr;
     void *carry = nullptr;
-    std::unordered_map<uint32_t, cudaGraphExec_t> graphs;  // by mask of groups present
+    cudaGraphExec_t graph = nullptr;  // all groups' batch kernels (ensure_graph)
     bool busy = false;
 };
 
@@ -115,8 +116,8 @@ struct Batch {
     sspmv_status st = SSPMV_OK;
 };
 
-// Device bytes a resident matrix holds (arrays; plans counted as merge
-// schedule + carries).
+// Device bytes a resident matrix holds (arrays; plans counted as chunk
+// starts + carries).
 int64_t device_bytes(const Matrix &M) {
     const int64_t V = (int64_t)vsize(M.vt), m = M.m, nnz = M.nnz;
     const int64_t plan = 2 * ((m + nnz) / 1024 + 2) * 152;
@@ -188,7 +189,8 @@ void release(Matrix &M) {
     if (M.ev) cudaEventDestroy(M.ev);
     M.ev = nullptr;
     M.ev_stream = nullptr;
-    M.coords[0] = M.coords[1] = nullptr;
+    M.row_start = nullptr;
+    M.batchable = false;
     M.resident = false;
 }
 
@@ -224,6 +226,7 @@ struct Server {
     sspmv_status make_room(int64_t need);
     sspmv_status ensure_resident(Matrix &M, bool *wait);
     void issue(Batch &b);
+    sspmv_status ensure_graph(Workspace &w);
     sspmv_status launch_groups(Workspace &w, uint32_t mask);
     void finish(Request *r, int32_t status, int64_t t);
 };
@@ -248,6 +251,8 @@ sspmv_status Server::init() {
     SSPMV_CUDA_TRY(cudaStreamCreateWithFlags(&load_stream, cudaStreamNonBlocking));
     SSPMV_CUDA_TRY(cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking));
     for (int g = 0; g < kBatchGroups; g++) csr_batch_grid(g);  // kernel attributes, before any capture
+    if (cfg.use_graphs && cfg.mode == SSPMV_SERVE_BATCHED)
+        for (auto &w : ws) SSPMV_TRY(ensure_graph(w));
     worker = std::thread([this] { worker_loop(); });
     completer = std::thread([this] { completion_loop(); });
     return SSPMV_OK;
@@ -272,7 +277,7 @@ void Server::shutdown() {
         if (kv.second->resident) release(*kv.second);
     for (auto &w : ws) {
         if (w.stream) cudaStreamSynchronize(w.stream);
-        for (auto &kv : w.graphs) cudaGraphExecDestroy(kv.second);
+        if (w.graph) cudaGraphExecDestroy(w.graph);
         cudaFree(w.d_in);
         cudaFree(w.d_out);
         cudaFreeHost(w.h_in);
@@ -314,8 +319,9 @@ sspmv_status Server::load(Matrix &M) {
     sspmv_status st = SSPMV_OK;
     if (M.fmt == SSPMV_FMT_CSR) {
         M.dev.csr = csr;
-        for (int w = 0; w < 2 && st == SSPMV_OK; w++)
-            st = csr_merge_coords(&M.dev.csr, w ? 8 : 1, &M.coords[w], &M.tiles[w], s);
+        int32_t gap = 0;
+        st = csr_stream_plan(&M.dev.csr, &M.row_start, &M.chunks, &gap, s);
+        M.batchable = st == SSPMV_OK && csr_stream_takes(M.nnz, gap);
     } else {
         st = convert(&csr, M, s);
         cudaStreamSynchronize(load_stream);
@@ -434,15 +440,16 @@ void Server::worker_loop() {
             r->y_bytes = M.m > 0 && !on_device ? (size_t)((M.m - 1) * r->r.ldy + k) * V : 0;
             r->stage_x = !on_device && (int64_t)r->x_bytes <= cfg.stage_limit_bytes;
             r->stage_y = !on_device && (int64_t)r->y_bytes <= cfg.stage_limit_bytes;
-            const bool batched = !per_request && M.fmt == SSPMV_FMT_CSR && (k == 1 || k == 2 || k == 4 || k == 8);
-            const int64_t t = batched ? M.tiles[k == 8 ? 1 : 0] : 0;
+            const bool batched = !per_request && M.fmt == SSPMV_FMT_CSR && M.batchable &&
+                                 (k == 1 || k == 2 || k == 4 || k == 8);
+            const int64_t t = batched ? M.chunks : 0;
             const size_t xa = up256(r->x_bytes), ya = up256(r->y_bytes);
             const bool fits = x_front + x_back + xa <= in_cap && y_front + y_back + ya <= out_bytes &&
                               tiles + t <= cfg.max_batch_tiles;
             if (!fits) {
                 std::lock_guard<std::mutex> g(mu);
                 if (b.reqs.empty()) {
-                    set_error("request on matrix %d needs more staging or merge tiles than one batch holds", M.id);
+                    set_error("request on matrix %d needs more staging or nonzero chunks than one batch holds", M.id);
                     finish(r, SSPMV_INVALID_ARG, now_ns());
                     cv_done.notify_all();
                     continue;
@@ -480,63 +487,65 @@ void Server::worker_loop() {
     }
 }
 
-sspmv_status Server::launch_groups(Workspace &w, uint32_t mask) {
+// The workspace's batch graph: every group's stream kernel and fix-up as
+// parallel branches (a group without requests in a batch exits at once), so
+// one graph serves every batch and is captured before the first one.
+// Captured on an idle stream (kernel arguments name only this workspace's
+// buffers); streams and events are made beforehand.
+sspmv_status Server::ensure_graph(Workspace &w) {
+    if (w.graph) return SSPMV_OK;
     BatchHeader *d_hdr = reinterpret_cast<BatchHeader *>(w.d_in);
     BatchItem *d_items = reinterpret_cast<BatchItem *>(w.d_in + sizeof(BatchHeader));
-    sspmv_stream_t s = reinterpret_cast<sspmv_stream_t>(w.stream);
+    std::vector<cudaStream_t> side(kBatchGroups - 1, nullptr);
+    std::vector<cudaEvent_t> evs(kBatchGroups, nullptr);  // [0]: fork, [1..]: joins
+    cudaError_t e = cudaSuccess;
+    for (auto &bs : side)
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking);
+    for (auto &ev : evs)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    sspmv_status st = SSPMV_OK;
+    cudaStream_t cs = capture_stream;
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaEventRecord(evs[0], cs);
+        for (int g = 0; g < kBatchGroups; g++) {
+            cudaStream_t bs = g == 0 ? cs : side[g - 1];
+            if (g > 0) cudaStreamWaitEvent(bs, evs[0], 0);
+            if (st == SSPMV_OK)
+                st = launch_csr_batch_group(g, d_hdr, d_items, w.carry, cfg.max_batch_tiles,
+                                            reinterpret_cast<sspmv_stream_t>(bs));
+            if (g > 0) {
+                cudaEventRecord(evs[g], bs);
+                cudaStreamWaitEvent(cs, evs[g], 0);
+            }
+        }
+        e = cudaStreamEndCapture(cs, &graph);
+        if (e == cudaSuccess && st == SSPMV_OK) e = cudaGraphInstantiate(&exec, graph, 0);
+    }
+    if (graph) cudaGraphDestroy(graph);
+    for (auto ev : evs)
+        if (ev) cudaEventDestroy(ev);
+    for (auto bs : side)
+        if (bs) cudaStreamDestroy(bs);
+    SSPMV_TRY(st);
+    if (e != cudaSuccess) return fail(SSPMV_CUDA_ERROR, "batch graph capture: %s", cudaGetErrorString(e));
+    w.graph = exec;
+    return SSPMV_OK;
+}
+
+sspmv_status Server::launch_groups(Workspace &w, uint32_t mask) {
     if (!cfg.use_graphs) {
+        BatchHeader *d_hdr = reinterpret_cast<BatchHeader *>(w.d_in);
+        BatchItem *d_items = reinterpret_cast<BatchItem *>(w.d_in + sizeof(BatchHeader));
+        sspmv_stream_t s = reinterpret_cast<sspmv_stream_t>(w.stream);
         for (int g = 0; g < kBatchGroups; g++)
             if (mask & (1u << g)) SSPMV_TRY(launch_csr_batch_group(g, d_hdr, d_items, w.carry, cfg.max_batch_tiles, s));
         return SSPMV_OK;
     }
-    auto it = w.graphs.find(mask);
-    if (it == w.graphs.end()) {
-        // One branch per group, forked from and joined back into the
-        // capturing stream, so the groups of one batch may run side by side.
-        // Captured on an idle stream (kernel arguments name only this
-        // workspace's buffers); streams and events are made beforehand.
-        const int ngroups = __builtin_popcount(mask);
-        std::vector<cudaStream_t> side(ngroups > 1 ? ngroups - 1 : 0, nullptr);
-        std::vector<cudaEvent_t> evs(ngroups, nullptr);  // [0]: fork, [1..]: joins
-        cudaError_t e = cudaSuccess;
-        for (auto &bs : side)
-            if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking);
-        for (auto &ev : evs)
-            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-        cudaGraph_t graph = nullptr;
-        cudaGraphExec_t exec = nullptr;
-        sspmv_status st = SSPMV_OK;
-        cudaStream_t cs = capture_stream;
-        if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-            cudaEventRecord(evs[0], cs);
-            int branch = 0;
-            for (int g = 0; g < kBatchGroups; g++) {
-                if (!(mask & (1u << g))) continue;
-                cudaStream_t bs = branch == 0 ? cs : side[branch - 1];
-                if (branch > 0) cudaStreamWaitEvent(bs, evs[0], 0);
-                if (st == SSPMV_OK)
-                    st = launch_csr_batch_group(g, d_hdr, d_items, w.carry, cfg.max_batch_tiles,
-                                                reinterpret_cast<sspmv_stream_t>(bs));
-                if (branch > 0) {
-                    cudaEventRecord(evs[branch], bs);
-                    cudaStreamWaitEvent(cs, evs[branch], 0);
-                }
-                branch++;
-            }
-            e = cudaStreamEndCapture(cs, &graph);
-            if (e == cudaSuccess && st == SSPMV_OK) e = cudaGraphInstantiate(&exec, graph, 0);
-        }
-        if (graph) cudaGraphDestroy(graph);
-        for (auto ev : evs)
-            if (ev) cudaEventDestroy(ev);
-        for (auto bs : side)
-            if (bs) cudaStreamDestroy(bs);
-        SSPMV_TRY(st);
-        if (e != cudaSuccess) return fail(SSPMV_CUDA_ERROR, "batch graph capture: %s", cudaGetErrorString(e));
-        it = w.graphs.emplace(mask, exec).first;
-    }
-    SSPMV_CUDA_TRY(cudaGraphLaunch(it->second, w.stream));
+    SSPMV_TRY(ensure_graph(w));
+    SSPMV_CUDA_TRY(cudaGraphLaunch(w.graph, w.stream));
     return SSPMV_OK;
 }
 
@@ -575,28 +584,31 @@ void Server::issue(Batch &b) {
         if (r->group < 0) continue;
         const int g = r->group;
         const Matrix &M = *r->mat;
-        const int which = r->r.k == 8 ? 1 : 0;
         BatchItem &it = items[hdr.item_begin[g] + fill[g]++];
         it.row_offset = M.dev.csr.row_offset;
         it.col_index = M.dev.csr.col_index;
         it.values = M.dev.csr.values;
-        it.coords = M.coords[which];
+        it.row_start = M.row_start;
         it.x = r->d_x;
         it.y = r->d_y;
         it.ldx = r->r.ldx;
         it.ldy = r->r.ldy;
         it.alpha = r->r.alpha;
         it.beta = r->r.beta;
-        it.tile_begin = group_tiles[g];
+        it.chunk_begin = group_tiles[g];
+        it.nnz = M.nnz;
         it.m = (int32_t)M.m;
-        it.num_tiles = (int32_t)M.tiles[which];
-        group_tiles[g] += M.tiles[which];
+        it.num_chunks = (int32_t)M.chunks;
+        it.vec = ((reinterpret_cast<uintptr_t>(M.dev.csr.col_index) | reinterpret_cast<uintptr_t>(M.dev.csr.values)) &
+                  15) == 0;
+        it.pad = 0;
+        group_tiles[g] += M.chunks;
         mask |= 1u << g;
     }
     int64_t carry = 0;
     for (int g = 0; g < kBatchGroups; g++) {
         hdr.n_items[g] = counts[g];
-        hdr.total_tiles[g] = group_tiles[g];
+        hdr.total_chunks[g] = group_tiles[g];
         hdr.carry_base[g] = carry;
         carry += group_tiles[g];
     }
@@ -708,7 +720,7 @@ extern "C" sspmv_status sspmv_server_create(const sspmv_server_config *cfg, sspm
     if (cfg) c = *cfg;
     if (c.mode != SSPMV_SERVE_BATCHED && c.mode != SSPMV_SERVE_PER_REQUEST) return fail(SSPMV_INVALID_ARG, "bad mode");
     if (c.max_batch_requests <= 0) c.max_batch_requests = 1024;
-    if (c.max_batch_tiles <= 0) c.max_batch_tiles = 1 << 17;
+    if (c.max_batch_tiles <= 0) c.max_batch_tiles = 1 << 20;
     if (c.arena_bytes <= 0) c.arena_bytes = 512ll << 20;
     if (c.stage_limit_bytes <= 0) c.stage_limit_bytes = 1 << 20;
     if (c.hbm_budget_bytes <= 0) c.hbm_budget_bytes = 120000000000ll;

@@ -3,7 +3,9 @@
 // Replaces LeSpMV_csr (src/spmv_csr.cpp:165-185) and its three CPU kernels
 // (serial, OpenMP per row, nnz-balanced row partition).
 //
-// Default kernel (kernel_flag 0 or 2): merge-path.  The (row end, nonzero)
+// Default kernel (kernel_flag 0 or 3): the nonzero-split stream kernel (see
+// csr_stream_kernel); matrices with long runs of empty rows fall back to
+// merge-path.  kernel_flag 2: merge-path.  The (row end, nonzero)
 // merge sequence is cut into equal tiles of kTile items, so every CTA does the
 // same work whatever the row lengths (power-law rows up to 50k nonzeros and
 // empty rows alike).  A CTA stages its nonzeros' products a_ij * x_j into
@@ -258,124 +260,6 @@ __global__ void csr_merge_fixup(int64_t num_tiles, int m, const int32_t *__restr
     for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
 }
 
-// ---------------------------------------------------- batched (serving) --
-// Index of the item owning global tile gt: the last item whose tile_begin is
-// <= gt (items of a group have increasing tile_begin).
-__device__ __forceinline__ int batch_item_of(const BatchItem *__restrict__ items, int n, int64_t gt) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (__ldg(&items[mid].tile_begin) <= gt) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
-// Persistent merge-path kernel over the tiles of every request of group g:
-// CTA b takes global tiles b, b + gridDim.x, ...  The tile body is the one
-// the single-matrix kernel runs, with the request's own split points, and
-// the carries go to per-batch slots, so results match a lone sspmv_LeSpMV_csr
-// / sspmv_spmm_csr call bit for bit.
-template <typename V, int K>
-__global__ void __launch_bounds__(kBlock) csr_batch_kernel(int g, const BatchHeader *__restrict__ hdr,
-                                                           const BatchItem *__restrict__ all_items,
-                                                           int32_t *__restrict__ carry_row,
-                                                           int32_t *__restrict__ has_end, V *__restrict__ carry_val,
-                                                           V *__restrict__ head_val) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int n = hdr->n_items[g];
-    const int64_t total = hdr->total_tiles[g];
-    const int64_t base = hdr->carry_base[g];
-    const BatchItem *items = all_items + hdr->item_begin[g];
-    for (int64_t gt = blockIdx.x; gt < total; gt += gridDim.x) {
-        const BatchItem *q = items + batch_item_of(items, n, gt);
-        const int64_t t = gt - q->tile_begin;
-        const int2 *coords = q->coords;
-        merge_tile<V, K>(q->m, q->row_offset, q->col_index, (const V *)q->values, (const V *)q->x, q->ldx,
-                         (V)q->alpha, (V)q->beta, (V *)q->y, q->ldy, coords[t], coords[t + 1], base + gt,
-                         carry_row, has_end, carry_val, head_val, smem_raw);
-    }
-}
-
-// The batched counterpart of csr_merge_fixup: one thread per global tile.
-template <typename V, int K>
-__global__ void csr_batch_fixup(int g, const BatchHeader *__restrict__ hdr, const BatchItem *__restrict__ all_items,
-                                const int32_t *__restrict__ carry_row, const int32_t *__restrict__ has_end,
-                                const V *__restrict__ carry_val, const V *__restrict__ head_val) {
-    const int n = hdr->n_items[g];
-    const int64_t total = hdr->total_tiles[g];
-    const int64_t base = hdr->carry_base[g];
-    const BatchItem *items = all_items + hdr->item_begin[g];
-    for (int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gt < total;
-         gt += (int64_t)gridDim.x * blockDim.x) {
-        const BatchItem *q = items + batch_item_of(items, n, gt);
-        const int64_t t = gt - q->tile_begin, nt = q->num_tiles;
-        if (nt <= 1) continue;
-        const int64_t slot = base + gt;
-        const int r = carry_row[slot];
-        if (r >= q->m) continue;
-        const int rs = q->row_offset[r];
-        if (rs < q->coords[t].y || rs >= q->coords[t + 1].y) continue;
-        V tot[K];
-#pragma unroll
-        for (int c = 0; c < K; c++) tot[c] = carry_val[slot * kMaxK + c];
-        for (int64_t u = t + 1; u < nt; u++) {
-            const int64_t su = slot + (u - t);
-            if (has_end[su]) {
-#pragma unroll
-                for (int c = 0; c < K; c++) tot[c] += head_val[su * kMaxK + c];
-                break;
-            }
-#pragma unroll
-            for (int c = 0; c < K; c++) tot[c] += carry_val[su * kMaxK + c];
-        }
-        V *yp = (V *)q->y + (int64_t)r * q->ldy;
-        const V alpha = (V)q->alpha, beta = (V)q->beta;
-#pragma unroll
-        for (int c = 0; c < K; c++) yp[c] = axpby(alpha, tot[c], beta, yp + c);
-    }
-}
-
-template <typename V, int K>
-size_t merge_smem_bytes() {
-    return (size_t)MergeShape<K>::tile * K * sizeof(V) + ((size_t)MergeShape<K>::tile + 1) * 4;
-}
-
-// Resident CTAs per SM of csr_batch_kernel<V, K> (sets its shared-memory
-// attribute on first use).
-template <typename V, int K>
-int batch_blocks_per_sm() {
-    static int blocks = 0;
-    if (blocks == 0) {
-        const size_t smem = merge_smem_bytes<V, K>();
-        cudaFuncSetAttribute(csr_batch_kernel<V, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        int b = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, csr_batch_kernel<V, K>, kBlock, smem) != cudaSuccess ||
-            b < 1)
-            b = 1;
-        blocks = b;
-    }
-    return blocks;
-}
-
-template <typename V, int K>
-sspmv_status launch_batch_vk(int g, const BatchHeader *hdr, const BatchItem *items, void *carry, int64_t slots,
-                             sspmv_stream_t s) {
-    unsigned char *c = (unsigned char *)carry;
-    int32_t *carry_row = (int32_t *)c;
-    int32_t *has_end = (int32_t *)(c + (size_t)slots * 4);
-    V *carry_val = (V *)(c + (size_t)slots * 8);
-    V *head_val = (V *)(c + (size_t)slots * (8 + kMaxK * 8));
-    const unsigned grid = (unsigned)(num_sms() * batch_blocks_per_sm<V, K>());
-    csr_batch_kernel<V, K><<<grid, kBlock, merge_smem_bytes<V, K>(), cu(s)>>>(g, hdr, items, carry_row, has_end,
-                                                                              carry_val, head_val);
-    SSPMV_LAUNCH_CHECK();
-    csr_batch_fixup<V, K><<<(unsigned)num_sms() * 2, 256, 0, cu(s)>>>(g, hdr, items, carry_row, has_end, carry_val,
-                                                                        head_val);
-    SSPMV_LAUNCH_CHECK();
-    return SSPMV_OK;
-}
-
 template <typename V, int K, int VS>
 __global__ void __launch_bounds__(kBlock) csr_vector_kernel(
     int m, const int32_t *__restrict__ row_offset, const int32_t *__restrict__ col_index,
@@ -480,11 +364,587 @@ sspmv_status launch_vector(const sspmv_csr *A, Plan *p, V alpha, const V *x, int
     }
 }
 
+// ------------------------------------------------------- stream kernel --
+// kernel_flag 3: nonzero-split "stream" kernel.  A warp takes 256 consecutive
+// nonzeros, lane l the 8 at 8l (vector loads of columns and values, all 8
+// gathers issued before use for k <= 2).  A lane finds the row of its first
+// nonzero by binary search inside the warp's row range (row_start of the
+// chunk, from the plan) and walks row_offset from there; a nonzero ends its
+// row when row_offset[r + 1] == e + 1.  Rows that start and end inside a lane
+// are written by it; the open sums before a lane's first row end and after
+// its last are joined by one segmented shuffle scan per warp, rows crossing
+// warps by a fix-up in chunk order (deterministic, no atomics).  The lane that
+// ends a row also writes the empty rows right after it (and the lane holding
+// nonzero 0 the empty rows before it); matrices with a run of more than
+// kStreamMaxGap empty rows use the merge-path kernel instead.
+constexpr int kStreamPerLane = 8;
+constexpr int kStreamChunk = 32 * kStreamPerLane;
+constexpr int kStreamMaxGap = 256;
+
+__global__ void stream_row_starts(int64_t nt, int m, int64_t nnz, const int32_t *__restrict__ rp,
+                                  int32_t *__restrict__ row_start) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > nt) return;
+    const int64_t e = t * kStreamChunk;
+    if (e >= nnz) {
+        row_start[t] = m;
+        return;
+    }
+    int lo = 0, hi = m - 1;  // last row r with rp[r] <= e: the row holding nonzero e
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (rp[mid] <= e) lo = mid;
+        else hi = mid - 1;
+    }
+    row_start[t] = lo;
+}
+
+// Longest run of empty rows (runs longer than kStreamMaxGap stop counting).
+__global__ void stream_max_gap(int m, const int32_t *__restrict__ rp, int *__restrict__ out) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        if (rp[i + 1] != rp[i] || (i > 0 && rp[i] == rp[i - 1])) continue;  // not the start of an empty run
+        int len = 0;
+        for (int64_t j = i; j < m && rp[j + 1] == rp[j] && len <= kStreamMaxGap; j++) len++;
+        atomicMax(out, len);
+    }
+}
+
+template <typename V>
+__device__ __forceinline__ void stream_load8(const int32_t *__restrict__ ci, const V *__restrict__ cv, int64_t e0,
+                                             int nv, bool vec, int (&c)[8], V (&a)[8]) {
+    if (vec && nv == 8) {
+        const int4 c0 = __ldcs(reinterpret_cast<const int4 *>(ci + e0));
+        const int4 c1 = __ldcs(reinterpret_cast<const int4 *>(ci + e0 + 4));
+        c[0] = c0.x; c[1] = c0.y; c[2] = c0.z; c[3] = c0.w; c[4] = c1.x; c[5] = c1.y; c[6] = c1.z; c[7] = c1.w;
+        if constexpr (sizeof(V) == 8) {
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const double2 v = __ldcs(reinterpret_cast<const double2 *>(cv + e0) + h);
+                a[2 * h] = v.x;
+                a[2 * h + 1] = v.y;
+            }
+        } else {
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const float4 v = __ldcs(reinterpret_cast<const float4 *>(cv + e0) + h);
+                a[4 * h] = v.x; a[4 * h + 1] = v.y; a[4 * h + 2] = v.z; a[4 * h + 3] = v.w;
+            }
+        }
+        return;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+        c[u] = u < nv ? ld_stream(ci + e0 + u) : 0;
+        a[u] = u < nv ? ld_stream(cv + e0 + u) : V(0);
+    }
+}
+
+// The stream kernel for k >= 4 right-hand sides: groups of G = k lanes
+// share a run of 8G consecutive nonzeros, lane q of a group owning column q,
+// so each gathered row X[col, 0:k] (k consecutive values) is read by G
+// adjacent lanes in one coalesced access instead of k scattered loads by one
+// lane.  A group walks its nonzeros in order (loads of 8 in flight) with the
+// row logic of the per-lane form; the groups' open sums are joined by a
+// segmented shuffle scan with stride G.
+template <typename V, int K, int G>
+__device__ __forceinline__ void stream_chunk_cols(
+    int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
+    const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
+    const int32_t *__restrict__ row_start, const int64_t w, const int64_t slot, int32_t *__restrict__ carry_row,
+    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val) {
+    static_assert(K % G == 0 && 32 % G == 0, "group shape");
+    constexpr int KL = K / G;                 // columns per lane
+    constexpr int NG = 32 / G;                // groups per warp
+    constexpr int EPG = kStreamChunk / NG;    // nonzeros per group (8G)
+    constexpr unsigned kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31, gi = lane / G, q0 = (lane % G) * KL;
+    const int64_t j0 = w * kStreamChunk;
+    if (j0 >= nnz) return;  // warp-uniform
+    const int64_t j1 = min(j0 + (int64_t)kStreamChunk, nnz);
+    const int64_t e0 = j0 + (int64_t)gi * EPG;
+    const int nv = (int)max((int64_t)0, min((int64_t)EPG, j1 - e0));
+    const int ra = __ldg(row_start + w);
+    const bool head_open = __ldg(rp + ra) < j0;
+    int r = ra;
+    if (nv > 0) {
+        int lo = ra, hi = min(__ldg(row_start + w + 1), m - 1);
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(rp + mid) <= e0) lo = mid;
+            else hi = mid - 1;
+        }
+        r = lo;
+    }
+    if (e0 == 0 && nv > 0) {  // empty rows before the first nonzero
+        for (int r2 = 0; r2 < r; r2++) {
+            V *yp = y + (int64_t)r2 * ldy + q0;
+#pragma unroll
+            for (int q = 0; q < KL; q++) yp[q] = axpby(alpha, V(0), beta, yp + q);
+        }
+    }
+    int rend = nv > 0 ? __ldg(rp + r + 1) : 0;
+    V seg[KL], head[KL];
+#pragma unroll
+    for (int q = 0; q < KL; q++) seg[q] = head[q] = V(0);
+    bool any_end = false, last_open = false;
+    int head_row = -1, last_row = -1;
+    for (int s0 = 0; s0 < nv; s0 += 8) {  // group-uniform
+        int c[8];
+        V a[8], xv[8][KL];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const bool ok = s0 + u < nv;
+            c[u] = ok ? ld_stream(ci + e0 + s0 + u) : 0;
+            a[u] = ok ? ld_stream(cv + e0 + s0 + u) : V(0);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int q = 0; q < KL; q++)
+                xv[u][q] = s0 + u < nv ? ld_x(x + (int64_t)c[u] * ldx + q0 + q) : V(0);
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            if (s0 + u < nv) {
+                const int64_t e = e0 + s0 + u;
+                while (rend <= e) rend = __ldg(rp + (++r) + 1);
+#pragma unroll
+                for (int q = 0; q < KL; q++) seg[q] += a[u] * xv[u][q];
+                last_row = r;
+                last_open = rend != e + 1;
+                if (!last_open) {
+                    if (!any_end) {
+                        any_end = true;
+                        head_row = r;
+#pragma unroll
+                        for (int q = 0; q < KL; q++) head[q] = seg[q];
+                    } else {
+                        V *yp = y + (int64_t)r * ldy + q0;
+#pragma unroll
+                        for (int q = 0; q < KL; q++) yp[q] = axpby(alpha, seg[q], beta, yp + q);
+                    }
+#pragma unroll
+                    for (int q = 0; q < KL; q++) seg[q] = V(0);
+                    for (int r2 = r + 1; r2 < m && __ldg(rp + r2 + 1) == e + 1; r2++) {
+                        V *yp = y + (int64_t)r2 * ldy + q0;
+#pragma unroll
+                        for (int q = 0; q < KL; q++) yp[q] = axpby(alpha, V(0), beta, yp + q);
+                    }
+                }
+            }
+        }
+    }
+    V S[KL];
+#pragma unroll
+    for (int q = 0; q < KL; q++) S[q] = seg[q];
+    bool f = any_end;
+#pragma unroll
+    for (int o = 1; o < NG; o <<= 1) {
+        V up[KL];
+#pragma unroll
+        for (int q = 0; q < KL; q++) up[q] = __shfl_up_sync(kFull, S[q], o * G);
+        const bool fu = __shfl_up_sync(kFull, f, o * G);
+        if (gi >= o) {
+            if (!f) {
+#pragma unroll
+                for (int q = 0; q < KL; q++) S[q] += up[q];
+            }
+            f = f || fu;
+        }
+    }
+    V cin[KL];
+#pragma unroll
+    for (int q = 0; q < KL; q++) {
+        cin[q] = __shfl_up_sync(kFull, S[q], G);
+        if (gi == 0) cin[q] = V(0);
+    }
+    if (any_end) {
+        V tot[KL];
+#pragma unroll
+        for (int q = 0; q < KL; q++) tot[q] = head[q] + cin[q];
+        if (head_row == ra && head_open) {
+            V *hp = head_val + slot * kMaxK + q0;
+#pragma unroll
+            for (int q = 0; q < KL; q++) hp[q] = tot[q];
+        } else {
+            V *yp = y + (int64_t)head_row * ldy + q0;
+#pragma unroll
+            for (int q = 0; q < KL; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
+        }
+    }
+    const bool chunk_end = __any_sync(kFull, any_end);
+    if (nv > 0 && e0 + nv == j1) {  // the group holding the chunk's last nonzero
+        if (q0 == 0) {
+            has_end[slot] = chunk_end ? 1 : 0;
+            carry_row[slot] = last_open ? last_row : -1;
+        }
+        if (last_open) {
+            V *cp = carry_val + slot * kMaxK + q0;
+#pragma unroll
+            for (int q = 0; q < KL; q++) cp[q] = S[q];
+        }
+    }
+}
+
+// Chunk w (nonzeros 256w ..) of one matrix, run by one warp; `slot` indexes
+// the carry arrays.  Shared by the single-matrix kernel and the batched
+// serving kernel.
+template <typename V, int K>
+__device__ __forceinline__ void stream_chunk_lanes(
+    int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
+    const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
+    const int32_t *__restrict__ row_start, const int64_t w, const int64_t slot, int32_t *__restrict__ carry_row,
+    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val, int vec) {
+    constexpr unsigned kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int64_t j0 = w * kStreamChunk;
+    if (j0 >= nnz) return;  // warp-uniform
+    const int64_t j1 = min(j0 + (int64_t)kStreamChunk, nnz);
+    const int64_t e0 = j0 + (int64_t)lane * kStreamPerLane;
+    const int nv = (int)max((int64_t)0, min((int64_t)kStreamPerLane, j1 - e0));
+    int c[8];
+    V a[8];
+    stream_load8<V>(ci, cv, e0, nv, vec != 0, c, a);
+    const int ra = __ldg(row_start + w);
+    const bool head_open = __ldg(rp + ra) < j0;  // the chunk's first row began in an earlier chunk
+    int r = ra;
+    if (nv > 0) {
+        int lo = ra, hi = min(__ldg(row_start + w + 1), m - 1);
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(rp + mid) <= e0) lo = mid;
+            else hi = mid - 1;
+        }
+        r = lo;
+    }
+    V xv[K <= 2 ? 8 : 1][K];
+    if constexpr (K <= 2) {
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int q = 0; q < K; q++) xv[u][q] = u < nv ? ld_x(x + (int64_t)c[u] * ldx + q) : V(0);
+    }
+    if (e0 == 0 && nv > 0) {  // empty rows before the first nonzero
+        for (int r2 = 0; r2 < r; r2++) {
+            V *yp = y + (int64_t)r2 * ldy;
+#pragma unroll
+            for (int q = 0; q < K; q++) yp[q] = axpby(alpha, V(0), beta, yp + q);
+        }
+    }
+    int rend = nv > 0 ? __ldg(rp + r + 1) : 0;
+    V seg[K], head[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) seg[q] = head[q] = V(0);
+    bool any_end = false, last_open = false;
+    int head_row = -1, last_row = -1;
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+        if (u < nv) {
+            const int64_t e = e0 + u;
+            while (rend <= e) rend = __ldg(rp + (++r) + 1);  // skip empty rows
+#pragma unroll
+            for (int q = 0; q < K; q++) {
+                if constexpr (K <= 2) seg[q] += a[u] * xv[u][q];
+                else seg[q] += a[u] * ld_x(x + (int64_t)c[u] * ldx + q);
+            }
+            last_row = r;
+            last_open = rend != e + 1;
+            if (!last_open) {  // row r ends at e
+                if (!any_end) {
+                    any_end = true;
+                    head_row = r;
+#pragma unroll
+                    for (int q = 0; q < K; q++) head[q] = seg[q];
+                } else {
+                    V *yp = y + (int64_t)r * ldy;
+#pragma unroll
+                    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, seg[q], beta, yp + q);
+                }
+#pragma unroll
+                for (int q = 0; q < K; q++) seg[q] = V(0);
+                for (int r2 = r + 1; r2 < m && __ldg(rp + r2 + 1) == e + 1; r2++) {  // empty rows after r
+                    V *yp = y + (int64_t)r2 * ldy;
+#pragma unroll
+                    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, V(0), beta, yp + q);
+                }
+            }
+        }
+    }
+    V S[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) S[q] = seg[q];
+    bool f = any_end;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        V up[K];
+#pragma unroll
+        for (int q = 0; q < K; q++) up[q] = __shfl_up_sync(kFull, S[q], o);
+        const bool fu = __shfl_up_sync(kFull, f, o);
+        if (lane >= o) {
+            if (!f) {
+#pragma unroll
+                for (int q = 0; q < K; q++) S[q] += up[q];
+            }
+            f = f || fu;
+        }
+    }
+    V cin[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        cin[q] = __shfl_up_sync(kFull, S[q], 1);
+        if (lane == 0) cin[q] = V(0);
+    }
+    if (any_end) {
+        V tot[K];
+#pragma unroll
+        for (int q = 0; q < K; q++) tot[q] = head[q] + cin[q];
+        if (head_row == ra && head_open) {
+            V *hp = head_val + slot * kMaxK;
+#pragma unroll
+            for (int q = 0; q < K; q++) hp[q] = tot[q];
+        } else {
+            V *yp = y + (int64_t)head_row * ldy;
+#pragma unroll
+            for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
+        }
+    }
+    const bool chunk_end = __any_sync(kFull, any_end);
+    if (nv > 0 && e0 + nv == j1) {  // the lane holding the chunk's last nonzero
+        has_end[slot] = chunk_end ? 1 : 0;
+        carry_row[slot] = last_open ? last_row : -1;
+        if (last_open) {
+            V *cp = carry_val + slot * kMaxK;
+#pragma unroll
+            for (int q = 0; q < K; q++) cp[q] = S[q];
+        }
+    }
+}
+
+// k <= 2: one lane per nonzero run (stream_chunk_lanes); k = 4, 8: column
+// groups (stream_chunk_cols).
+template <typename V, int K>
+__device__ __forceinline__ void stream_chunk(
+    int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
+    const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
+    const int32_t *__restrict__ row_start, const int64_t w, const int64_t slot, int32_t *__restrict__ carry_row,
+    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val, int vec) {
+    if constexpr (K >= 4)
+        stream_chunk_cols<V, K, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, slot, carry_row,
+                                   has_end, carry_val, head_val);
+    else
+        stream_chunk_lanes<V, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, slot, carry_row,
+                                 has_end, carry_val, head_val, vec);
+}
+
+template <typename V, int K>
+__global__ void __launch_bounds__(kBlock) csr_stream_kernel(
+    int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
+    const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
+    const int32_t *__restrict__ row_start, int32_t *__restrict__ carry_row, int32_t *__restrict__ has_end,
+    V *__restrict__ carry_val, V *__restrict__ head_val, int vec) {
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    stream_chunk<V, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, w, carry_row, has_end,
+                       carry_val, head_val, vec);
+}
+
+// Rows crossing chunks: the chunk where the row starts adds the later
+// chunks' pieces in order.
+template <typename V, int K>
+__global__ void csr_stream_fixup(int64_t nt, const int32_t *__restrict__ rp, const int32_t *__restrict__ carry_row,
+                                 const int32_t *__restrict__ has_end, const V *__restrict__ carry_val,
+                                 const V *__restrict__ head_val, V alpha, V beta, V *__restrict__ y, int64_t ldy) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const int r = carry_row[t];
+    if (r < 0 || (int64_t)rp[r] < t * kStreamChunk) return;  // not open here, or began in an earlier chunk
+    V tot[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) tot[q] = carry_val[t * kMaxK + q];
+    for (int64_t u = t + 1; u < nt; u++) {
+        if (has_end[u]) {
+#pragma unroll
+            for (int q = 0; q < K; q++) tot[q] += head_val[u * kMaxK + q];
+            break;
+        }
+#pragma unroll
+        for (int q = 0; q < K; q++) tot[q] += carry_val[u * kMaxK + q];
+    }
+    V *yp = y + (int64_t)r * ldy;
+#pragma unroll
+    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
+}
+
+// Plan slots of the stream kernel (CSR matrices use no other extra slots):
+// extra[0] row_start[nt + 1], extra[1] carry_row/has_end [2 nt], extra[2]
+// carry values, extra[3] head values; extra_i[0] = nt, extra_i[1] = longest
+// empty-row run (capped just above kStreamMaxGap).
+sspmv_status ensure_stream_plan(const sspmv_csr *A, Plan *p, sspmv_stream_t s) {
+    if (p->extra[0]) return SSPMV_OK;
+    std::lock_guard<std::mutex> g(plan_mutex());
+    if (p->extra[0]) return SSPMV_OK;
+    const int64_t m = A->f.num_rows, nnz = A->f.num_nnzs;
+    const int64_t nt = std::max<int64_t>((nnz + kStreamChunk - 1) / kStreamChunk, 1);
+    const size_t sv = vsize(A->f.value_type);
+    int32_t *starts = nullptr, *ints = nullptr;
+    unsigned char *cvals = nullptr, *hvals = nullptr;
+    int *gap = nullptr;
+    SSPMV_TRY(dalloc(&starts, (size_t)nt + 1, s));
+    SSPMV_TRY(dalloc(&ints, (size_t)nt * 2, s));
+    SSPMV_TRY(dalloc(&cvals, (size_t)nt * kMaxK * sv, s));
+    SSPMV_TRY(dalloc(&hvals, (size_t)nt * kMaxK * sv, s));
+    SSPMV_TRY(dalloc(&gap, 1, s));
+    SSPMV_CUDA_TRY(cudaMemsetAsync(gap, 0, sizeof(int), cu(s)));
+    stream_row_starts<<<grid_for(nt + 1, 256), 256, 0, cu(s)>>>(nt, (int)m, nnz, A->row_offset, starts);
+    SSPMV_LAUNCH_CHECK();
+    stream_max_gap<<<grid_for(m, 256, (int64_t)num_sms() * 16), 256, 0, cu(s)>>>((int)m, A->row_offset, gap);
+    SSPMV_LAUNCH_CHECK();
+    int hgap = 0;
+    SSPMV_CUDA_TRY(cudaMemcpyAsync(&hgap, gap, sizeof(int), cudaMemcpyDeviceToHost, cu(s)));
+    SSPMV_CUDA_TRY(cudaStreamSynchronize(cu(s)));
+    dfree(gap, s);
+    p->extra_i[0] = nt;
+    p->extra_i[1] = hgap;
+    p->extra[1] = ints;
+    p->extra[2] = cvals;
+    p->extra[3] = hvals;
+    p->extra[0] = starts;  // published last
+    return SSPMV_OK;
+}
+
+template <typename V, int K>
+sspmv_status launch_stream(const sspmv_csr *A, Plan *p, V alpha, const V *x, int64_t ldx, V beta, V *y,
+                           int64_t ldy, sspmv_stream_t s) {
+    if (A->f.num_nnzs == 0) return launch_merge<V, K>(A, p, alpha, x, ldx, beta, y, ldy, s);
+    SSPMV_TRY(ensure_stream_plan(A, p, s));
+    if (p->extra_i[1] > kStreamMaxGap) return launch_merge<V, K>(A, p, alpha, x, ldx, beta, y, ldy, s);
+    const int64_t nt = p->extra_i[0];
+    int32_t *ints = (int32_t *)p->extra[1];
+    const int vec = ((reinterpret_cast<uintptr_t>(A->col_index) | reinterpret_cast<uintptr_t>(A->values)) & 15) == 0;
+    csr_stream_kernel<V, K><<<grid_for(nt * 32, kBlock), kBlock, 0, cu(s)>>>(
+        (int)A->f.num_rows, A->f.num_nnzs, A->row_offset, A->col_index, (const V *)A->values, x, ldx, alpha, beta,
+        y, ldy, (const int32_t *)p->extra[0], ints, ints + nt, (V *)p->extra[2], (V *)p->extra[3], vec);
+    SSPMV_LAUNCH_CHECK();
+    if (nt > 1) {
+        csr_stream_fixup<V, K><<<grid_for(nt, 256), 256, 0, cu(s)>>>(nt, A->row_offset, ints, ints + nt,
+                                                                     (const V *)p->extra[2], (const V *)p->extra[3],
+                                                                     alpha, beta, y, ldy);
+        SSPMV_LAUNCH_CHECK();
+    }
+    return SSPMV_OK;
+}
+
+// ---------------------------------------------------- batched (serving) --
+// Index of the item owning global chunk gc: the last item whose chunk_begin
+// is <= gc (items of a group have increasing chunk_begin).
+__device__ __forceinline__ int batch_item_of(const BatchItem *__restrict__ items, int n, int64_t gc) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&items[mid].chunk_begin) <= gc) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Persistent stream kernel over the chunks of every request of group g:
+// warp i of the grid takes global chunks i, i + warps, ...  A request is cut
+// into the chunks a lone sspmv_spmm_csr call uses (the matrix's own
+// row_start), and its carries go to per-batch slots, so its result does not
+// depend on the rest of the batch and equals the single-request call's.
+template <typename V, int K>
+__global__ void __launch_bounds__(kBlock) csr_batch_kernel(int g, const BatchHeader *__restrict__ hdr,
+                                                           const BatchItem *__restrict__ all_items,
+                                                           int32_t *__restrict__ carry_row,
+                                                           int32_t *__restrict__ has_end, V *__restrict__ carry_val,
+                                                           V *__restrict__ head_val) {
+    const int n = hdr->n_items[g];
+    const int64_t total = hdr->total_chunks[g];
+    const int64_t base = hdr->carry_base[g];
+    const BatchItem *items = all_items + hdr->item_begin[g];
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t gc = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; gc < total; gc += warps) {
+        const BatchItem *q = items + batch_item_of(items, n, gc);
+        stream_chunk<V, K>(q->m, q->nnz, q->row_offset, q->col_index, (const V *)q->values, (const V *)q->x, q->ldx,
+                           (V)q->alpha, (V)q->beta, (V *)q->y, q->ldy, q->row_start, gc - q->chunk_begin, base + gc,
+                           carry_row, has_end, carry_val, head_val, q->vec);
+    }
+}
+
+// The batched counterpart of csr_stream_fixup: one thread per global chunk.
+template <typename V, int K>
+__global__ void csr_batch_fixup(int g, const BatchHeader *__restrict__ hdr, const BatchItem *__restrict__ all_items,
+                                const int32_t *__restrict__ carry_row, const int32_t *__restrict__ has_end,
+                                const V *__restrict__ carry_val, const V *__restrict__ head_val) {
+    const int n = hdr->n_items[g];
+    const int64_t total = hdr->total_chunks[g];
+    const int64_t base = hdr->carry_base[g];
+    const BatchItem *items = all_items + hdr->item_begin[g];
+    for (int64_t gc = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gc < total;
+         gc += (int64_t)gridDim.x * blockDim.x) {
+        const BatchItem *q = items + batch_item_of(items, n, gc);
+        const int64_t t = gc - q->chunk_begin, nt = q->num_chunks;
+        if (nt <= 1) continue;
+        const int64_t slot = base + gc;
+        const int r = carry_row[slot];
+        if (r < 0 || (int64_t)q->row_offset[r] < t * kStreamChunk) continue;
+        V tot[K];
+#pragma unroll
+        for (int c = 0; c < K; c++) tot[c] = carry_val[slot * kMaxK + c];
+        for (int64_t u = t + 1; u < nt; u++) {
+            const int64_t su = slot + (u - t);
+            if (has_end[su]) {
+#pragma unroll
+                for (int c = 0; c < K; c++) tot[c] += head_val[su * kMaxK + c];
+                break;
+            }
+#pragma unroll
+            for (int c = 0; c < K; c++) tot[c] += carry_val[su * kMaxK + c];
+        }
+        V *yp = (V *)q->y + (int64_t)r * q->ldy;
+        const V alpha = (V)q->alpha, beta = (V)q->beta;
+#pragma unroll
+        for (int c = 0; c < K; c++) yp[c] = axpby(alpha, tot[c], beta, yp + c);
+    }
+}
+
+// Resident CTAs per SM of csr_batch_kernel<V, K>.
+template <typename V, int K>
+int batch_blocks_per_sm() {
+    static int blocks = 0;
+    if (blocks == 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, csr_batch_kernel<V, K>, kBlock, 0) != cudaSuccess ||
+            b < 1)
+            b = 1;
+        blocks = b;
+    }
+    return blocks;
+}
+
+template <typename V, int K>
+sspmv_status launch_batch_vk(int g, const BatchHeader *hdr, const BatchItem *items, void *carry, int64_t slots,
+                             sspmv_stream_t s) {
+    unsigned char *c = (unsigned char *)carry;
+    int32_t *carry_row = (int32_t *)c;
+    int32_t *has_end = (int32_t *)(c + (size_t)slots * 4);
+    V *carry_val = (V *)(c + (size_t)slots * 8);
+    V *head_val = (V *)(c + (size_t)slots * (8 + kMaxK * 8));
+    const unsigned grid = (unsigned)(num_sms() * batch_blocks_per_sm<V, K>());
+    csr_batch_kernel<V, K><<<grid, kBlock, 0, cu(s)>>>(g, hdr, items, carry_row, has_end, carry_val, head_val);
+    SSPMV_LAUNCH_CHECK();
+    csr_batch_fixup<V, K><<<(unsigned)num_sms() * 2, 256, 0, cu(s)>>>(g, hdr, items, carry_row, has_end, carry_val,
+                                                                        head_val);
+    SSPMV_LAUNCH_CHECK();
+    return SSPMV_OK;
+}
+
+// kernel_flag 0 (default) and 3: stream kernel (merge-path for matrices it
+// does not take); 2: merge-path; 1: vector.
 template <typename V, int K>
 sspmv_status csr_pass(const sspmv_csr *A, Plan *p, V alpha, const V *x, int64_t ldx, V beta, V *y,
                       int64_t ldy, sspmv_stream_t s) {
     if (A->f.kernel_flag == 1) return launch_vector<V, K>(A, p, alpha, x, ldx, beta, y, ldy, s);
-    return launch_merge<V, K>(A, p, alpha, x, ldx, beta, y, ldy, s);
+    if (A->f.kernel_flag == 2) return launch_merge<V, K>(A, p, alpha, x, ldx, beta, y, ldy, s);
+    return launch_stream<V, K>(A, p, alpha, x, ldx, beta, y, ldy, s);
 }
 
 }  // namespace
@@ -543,18 +1003,18 @@ sspmv_status ensure_merge_plan(Plan *p, int which, int64_t m, int64_t nnz, const
     return SSPMV_OK;
 }
 
-int csr_merge_tile_items(int32_t k) { return k > 4 ? MergeShape<8>::tile : MergeShape<1>::tile; }
-
-sspmv_status csr_merge_coords(const sspmv_csr *A, int32_t k, const int2 **coords, int64_t *num_tiles,
-                              sspmv_stream_t s) {
+sspmv_status csr_stream_plan(const sspmv_csr *A, const int32_t **row_start, int64_t *num_chunks, int32_t *max_gap,
+                             sspmv_stream_t s) {
     Plan *p = get_plan(&A->f);
     if (!p) return fail(SSPMV_OUT_OF_MEMORY, "plan allocation failed");
-    const int which = k > 4 ? 1 : 0;
-    SSPMV_TRY(ensure_merge_plan(p, which, A->f.num_rows, A->f.num_nnzs, A->row_offset, A->f.value_type, s));
-    *coords = p->merge[which].coords;
-    *num_tiles = p->merge[which].num_tiles;
+    SSPMV_TRY(ensure_stream_plan(A, p, s));
+    *row_start = (const int32_t *)p->extra[0];
+    *num_chunks = p->extra_i[0];
+    *max_gap = (int32_t)p->extra_i[1];
     return SSPMV_OK;
 }
+
+bool csr_stream_takes(int64_t num_nnzs, int32_t max_gap) { return num_nnzs > 0 && max_gap <= kStreamMaxGap; }
 
 unsigned csr_batch_grid(int g) {
     int b = 1;

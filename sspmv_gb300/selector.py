@@ -15,7 +15,8 @@ the GPU through the library:
     layer, loss and Adam kernels (sspmv_nn_*), PyTorch tensors only holding
     the memory;
   - decision: the format with the best predicted time among those feasible
-    for the matrix, plain CSR when the prediction is not better than CSR.
+    for the matrix, plain CSR when no format is predicted faster than CSR
+    (rule "time"; rule "class" takes the most likely class instead).
 Regret of a pick = its measured time / the fastest measured time - 1.
 """
 from __future__ import annotations
@@ -40,7 +41,7 @@ NUM_DIAGS = 43  # index of num_diags in the feature vector
 
 # Parameter sets tried per format when labelling (library defaults first).
 LABEL_CANDIDATES = {
-    "csr": [("kernel", 0, 0), ("kernel", 1, 0), ("kernel", 1, 4), ("kernel", 1, 32)],
+    "csr": [("kernel", 0, 0), ("kernel", 2, 0), ("kernel", 1, 2), ("kernel", 1, 8), ("kernel", 1, 32)],
     "coo": [("kernel", 0, 0), ("kernel", 1, 0)],
     "ell": [{}],
     "sell": [dict(chunkwidth=8, alignment=0), dict(chunkwidth=32, alignment=0)],
@@ -118,6 +119,9 @@ def raw_features(csr) -> np.ndarray:
 def model_inputs(raw: np.ndarray) -> np.ndarray:
     """Raw features and their signed logs (rows = matrices)."""
     raw = np.atleast_2d(np.asarray(raw, np.float64))
+    # symmetry ratios are 0/0 for matrices without off-diagonal entries, and
+    # value maxima start at -DBL_MAX when a matrix has no such entry
+    raw = np.clip(np.nan_to_num(raw, nan=0.0, posinf=1e30, neginf=-1e30), -1e30, 1e30)
     return np.concatenate([raw, np.sign(raw) * np.log1p(np.abs(raw))], axis=1)
 
 
@@ -378,7 +382,7 @@ def train(ds: Dataset, train_idx, epochs: int = 400, batch: int = 128, lr: float
     return net
 
 
-def choose(net: MLP, raw: np.ndarray, feasible: np.ndarray | None = None, rule: str = "class") -> np.ndarray:
+def choose(net: MLP, raw: np.ndarray, feasible: np.ndarray | None = None, rule: str = "time") -> np.ndarray:
     """Format label per matrix.  rule "class": the most likely feasible class,
     kept only when the time head does not predict it slower than CSR
     (otherwise CSR).  rule "time": the best predicted time among feasible
@@ -422,22 +426,72 @@ def evaluate(ds: Dataset, train_frac: float = 0.8, seed: int = 0, epochs: int = 
     net = train(ds, tr, epochs=epochs, seed=seed, log=log)
     train_s = time.perf_counter() - t0
     feas = np.isfinite(ds.times[te])
-    picks = choose(net, ds.raw[te], feas, "class")
+    picks = choose(net, ds.raw[te], feas, "time")
     res = regret(ds.times[te], picks)
-    res["time_rule"] = regret(ds.times[te], choose(net, ds.raw[te], feas, "time"))
+    res["class_rule"] = regret(ds.times[te], choose(net, ds.raw[te], feas, "class"))
     res.update({"train": int(ntr), "test": int(len(te)), "train_s": round(train_s, 2),
                 "label_hist": np.bincount(ds.labels, minlength=NUM_CLASSES).tolist(),
                 "pick_hist": np.bincount(picks, minlength=NUM_CLASSES).tolist()})
     return net, res
 
 
-def save_model(net: MLP, path: str | Path) -> None:
-    np.savez(path, **net.state())
+def save_model(net: MLP, path: str | Path, params: dict | None = None) -> None:
+    d = net.state()
+    d["format_params"] = np.frombuffer(json.dumps(params or {}).encode(), np.uint8)
+    np.savez(path, **d)
 
 
 def load_model(path: str | Path) -> MLP:
     d = dict(np.load(path))
+    d.pop("format_params", None)
     return MLP.from_state(d)
+
+
+MAX_ROW = 7     # feature index: longest row
+NUM_ROWS = 0
+NUM_NNZ = 2
+
+
+def feasible_from_features(raw: np.ndarray) -> np.ndarray:
+    """Formats that can be built for each matrix, from its features alone
+    (the labelling rules: ELL padding within 4x, DIA within 10240 diagonals
+    and 8x padding).  BSR is decided by its converter at load time."""
+    raw = np.atleast_2d(raw)
+    m, nnz = raw[:, NUM_ROWS], np.maximum(raw[:, NUM_NNZ], 1)
+    f = np.ones((len(raw), NUM_CLASSES), bool)
+    f[:, LABELS.index("ell")] = raw[:, MAX_ROW] * m <= 4 * nnz
+    nd = raw[:, NUM_DIAGS]
+    f[:, LABELS.index("dia")] = (nd <= 10240) & (nd * m <= 8 * nnz)
+    return f
+
+
+def common_params(paths) -> dict:
+    """Most frequent best parameter set per format in labelled data."""
+    from collections import Counter
+    cnt = {f: Counter() for f in LABELS}
+    for p in ([paths] if isinstance(paths, (str, Path)) else paths):
+        for ln in Path(p).read_text().splitlines():
+            if ln.strip():
+                r = json.loads(ln)
+                for f, prm in r["params"].items():
+                    if prm is not None:
+                        cnt[f][json.dumps(prm, sort_keys=True)] += 1
+    return {f: json.loads(c.most_common(1)[0][0]) for f, c in cnt.items() if c}
+
+
+class Selector:
+    """A trained network and the parameter set it uses per format; picks the
+    serving format of a device CSR matrix."""
+
+    def __init__(self, path: str | Path):
+        d = dict(np.load(path))
+        self.params = json.loads(bytes(d.pop("format_params", np.zeros(2, np.uint8))).decode() or "{}")
+        self.net = MLP.from_state(d)
+
+    def pick(self, csr) -> tuple[str, dict | None]:
+        raw = raw_features(csr)[None, :]
+        fmt = LABELS[int(choose(self.net, raw, feasible_from_features(raw))[0])]
+        return fmt, self.params.get(fmt)
 
 
 def main(argv=None) -> None:
@@ -473,7 +527,7 @@ def main(argv=None) -> None:
     ds = load_dataset(a.data)
     net, res = evaluate(ds, 0.8, a.seed, a.epochs, log)
     res["matrices"] = int(len(ds.ids))
-    save_model(net, a.model)
+    save_model(net, a.model, common_params(a.data))
     Path(a.report).write_text(json.dumps(res, indent=1) + "\n")
     log(json.dumps(res))
 

@@ -4,7 +4,7 @@ A `Server` keeps registered matrices resident in HBM in their serving format
 (least-recently-used eviction under a byte budget) and serves SpMV / SpMM
 requests y = alpha*A*X + beta*Y with continuous batching: requests that
 arrive while batches run on the GPU are gathered into the next batch, whose
-CSR requests (k in 1, 2, 4, 8) run in one persistent merge-path launch per
+CSR requests (k in 1, 2, 4, 8) run in one persistent stream-kernel launch per
 (value type, k) group replayed from a CUDA graph.  mode="per_request" serves
 each request with its own sspmv_spmm_<fmt> launch instead (the comparison
 point).
@@ -287,22 +287,68 @@ class ServingBench:
         return out
 
 
+# converter integer arguments in sspmv_server_add_matrix order, from the
+# keyword names the Python converters take
+_PARAM_ORDER = {"ell": ["ld"], "sell": ["chunkwidth", "alignment"],
+                "sell_c_sigma": ["slicewidth", "chunkwidth", "alignment"], "sell_c_R": ["chunkwidth", "alignment"],
+                "dia": ["max_diags", "alignment"], "bsr": ["blockDimRow", "blockDimCol"], "csr5": ["sigma", "omega"]}
+
+
+def server_params(fmt: str, params: dict | None) -> list[int] | None:
+    if fmt not in _PARAM_ORDER or not params:
+        return None
+    return [int(params.get(k, 0)) for k in _PARAM_ORDER[fmt]]
+
+
+def select_formats(mats: list[dict], model_path, min_nnz: int = 1_000_000, log=None) -> list[tuple[str, list | None]]:
+    """Serving format of each matrix: the selector's pick for matrices with
+    at least min_nnz nonzeros (their kernel time dwarfs a launch), CSR --
+    batched with the other requests -- for the rest."""
+    from . import lespmv as L
+    from .selector import Selector
+    sel = Selector(model_path)
+    out = []
+    for d in mats:
+        A = d["A"]
+        if A.nnz < min_nnz:
+            out.append(("csr", None))
+            continue
+        csr = L.csr_from_host(A)
+        fmt, prm = sel.pick(csr)
+        csr.delete()
+        out.append((fmt, server_params(fmt, prm)))
+        if log:
+            log(f"[serving] {d['family']} n={A.num_rows} nnz={A.nnz}: {fmt} {prm}")
+    return out
+
+
 def serving_benchmark(num_matrices: int = 64, device_buffers: bool = False, duration_s: float = 1.5,
-                      seed: int = 0, log=None) -> dict:
+                      seed: int = 0, log=None, selector_model=None) -> dict:
     """Saturation throughput of the batched server and of per-request CSR
     launches, then p50/p99 under Poisson load swept up to saturation.
     'Equal p99' compares throughput at the per-request server's p99 at 70% of
     its saturation rate."""
     log = log or (lambda *a: None)
     b = ServingBench(num_matrices, seed, device_buffers, log)
+    picks = select_formats(b.mats, selector_model, log=log) if selector_model else None
     res = {"matrices": num_matrices, "registered": 2 * num_matrices, "total_nnz_per_precision": b.total_nnz,
            "buffers": "device" if device_buffers else "pinned host", "modes": {},
            "server_config": {"per_request": {"num_inflight": 8, "arena_bytes": 160 << 20},
                              "batched": {"num_inflight": 3, "arena_bytes": 512 << 20}}}
     # Per-request launches get more requests in flight (they cannot batch).
     server_kw = res["server_config"]
+    if picks:
+        res["formats"] = {f"{d['family']}:{d['n']}": pk[0] for d, pk in zip(b.mats, picks) if pk[0] != "csr"}
+
+    def fmt_of(mode):
+        # the per-request comparison point is plain CSR; the batched server
+        # serves each matrix in its selected format
+        if mode == "per_request" or not picks:
+            return None
+        return lambda mid, A: picks[mid // 2]
+
     for mode in ("per_request", "batched"):
-        s = b.server(mode, **server_kw[mode])
+        s = b.server(mode, fmt_of(mode), **server_kw[mode])
         try:
             b.run(s, 2000, 0.0, seed + 1)  # warm: graphs for the group sets, pools
             sat = b.run(s, 20000 if mode == "batched" else 8000, 0.0, seed + 2)

@@ -89,3 +89,9 @@ def test_mtx_errors_are_statuses(tmp_path):
     assert e.value.status == 7
     with pytest.raises(_lib.SSPMVError):
         read_csr_matrix(tmp_path / "missing.mtx")
+
+
+def test_torch_operator_is_registered():
+    import torch
+    import sspmv_gb300.torch_ops  # noqa: F401
+    assert hasattr(torch.ops.sspmv, "spmv_csr")

@@ -21,7 +21,7 @@ def _csr(A):
     return csr_from_host(A)
 
 
-@pytest.mark.parametrize("flag", [0, 1])
+@pytest.mark.parametrize("flag", [0, 1, 3])
 @pytest.mark.parametrize("path", CASES, ids=[p.stem for p in CASES])
 def test_csr_golden(path, flag, oracle_lib):
     from sspmv_gb300.lespmv import LeSpMV_csr
@@ -58,7 +58,7 @@ def test_csr_spmm_families(fam, k, dt, oracle_lib):
     X = synth.vector(A.num_cols, 0, dt, k).reshape(A.num_cols, k)
     Y0 = synth.vector(A.num_rows, 7, dt, k).reshape(A.num_rows, k)
     M = _csr(A)
-    for flag in (0, 1):
+    for flag in (0, 1, 3):
         M.kernel_flag = flag
         Y = to_dev(Y0)
         spmm(ALPHA, M, to_dev(X), BETA, Y)

@@ -61,3 +61,21 @@ def test_regret_arithmetic():
     r = regret(times, np.array([2, CSR_LABEL]))  # infeasible pick falls back to CSR
     assert np.isclose(r["mean_regret"], ((2.0 / 1.0 - 1) + (1.5 / 1.0 - 1)) / 2)
     assert np.isclose(r["csr_mean_regret"], r["mean_regret"])
+
+
+def test_feasibility_from_features_and_server_params():
+    from sspmv_gb300.selector import LABELS, NUM_DIAGS, feasible_from_features
+    from sspmv_gb300.serving import server_params
+    raw = np.zeros((3, 66))
+    raw[:, 0] = 1000           # rows
+    raw[:, 2] = 10000          # nonzeros
+    raw[:, 7] = [10, 41, 10]   # longest row: ELL pads 1x, 4.1x, 1x
+    raw[:, NUM_DIAGS] = [9, 9, 20000]
+    f = feasible_from_features(raw)
+    ell, dia = LABELS.index("ell"), LABELS.index("dia")
+    assert f[0, ell] and not f[1, ell] and f[2, ell]
+    assert f[0, dia] and f[1, dia] and not f[2, dia]
+    assert f[:, LABELS.index("csr")].all()
+    assert server_params("sell_c_sigma", {"slicewidth": 256, "chunkwidth": 8, "alignment": 0}) == [256, 8, 0]
+    assert server_params("bsr", {"blockDimRow": 2, "blockDimCol": 4}) == [2, 4]
+    assert server_params("csr", {"kernel_flag": 1, "param": 4}) is None

@@ -74,3 +74,29 @@ def test_noalloc_rejects_matrices_past_its_limit():
     st = _noalloc(1.0, M, x, 0.0, x)
     assert st == 1  # SSPMV_INVALID_ARG
     assert b"limit" in _lib.lib.sspmv_last_error()
+
+
+@pytest.mark.gpu
+def test_torch_custom_op_matches_library_call():
+    """torch.ops.sspmv.spmv_csr (stateless, on the no-allocation entry point)
+    equals sspmv_LeSpMV_csr with the merge-path kernel bit for bit, 1-D and
+    2-D x."""
+    import torch
+    import sspmv_gb300.torch_ops  # noqa: F401  (registers the operator)
+    from sspmv_gb300 import synth
+    from sspmv_gb300.lespmv import LeSpMV_csr, csr_from_host
+    for dt in (np.float64, np.float32):
+        A = synth.generate(synth.powerlaw(30000, 1.8, 16.0, 20000, 0.05), 9, dt)
+        rp = torch.from_numpy(A.row_offset).cuda()
+        ci = torch.from_numpy(A.col_index).cuda()
+        cv = torch.from_numpy(A.values).cuda()
+        X = torch.from_numpy(synth.vector(A.num_cols, 0, dt, 3).reshape(A.num_cols, 3)).cuda()
+        Y = torch.ops.sspmv.spmv_csr(rp, ci, cv, A.num_cols, X)
+        y1 = torch.ops.sspmv.spmv_csr(rp, ci, cv, A.num_cols, X[:, 1].contiguous())
+        M = csr_from_host(A)
+        M.kernel_flag = 2  # the merge-path kernel the allocation-free entry point runs
+        for j in range(3):
+            ref = torch.zeros(A.num_rows, dtype=cv.dtype, device="cuda")
+            LeSpMV_csr(1.0, M, X[:, j].contiguous(), 0.0, ref)
+            assert torch.equal(Y[:, j], ref)
+        assert torch.equal(y1, Y[:, 1])
