@@ -52,6 +52,9 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (library defaults)")
     ap.add_argument("--csr-kernel", default="", help="pin the CSR kernel as FLAG:PARAM (implies no tuning of CSR)")
+    ap.add_argument("--kernel", action="append", default=[],
+                    help="pin a format's kernel as FMT:FLAG:PARAM (repeatable; that format is not tuned)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-large", action="store_true", help="skip the power-law 16M SELL-c-sigma vs CSR section")
     ap.add_argument("--no-serving", action="store_true", help="skip the request-server section")
     return ap.parse_args()
@@ -180,16 +183,20 @@ def run_gpu(args, rank, world):
                               "rows": A.num_rows, "cols": A.num_cols})
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
+    pinned = {}
     if args.csr_kernel:
-        flag, param = (int(v) for v in args.csr_kernel.split(":"))
-        for c in cases:
-            if c["fmt"] == "csr":
-                c["M"].set_kernel(flag, param)
+        pinned["csr"] = tuple(int(v) for v in args.csr_kernel.split(":"))
+    for spec in args.kernel:
+        fmt, flag, param = spec.split(":")
+        pinned[fmt] = (int(flag), int(param))
+    for c in cases:
+        if c["fmt"] in pinned:
+            c["M"].set_kernel(*pinned[c["fmt"]])
     if not args.no_tune:
         from sspmv_gb300 import autotune
         seen = set()
         for c in cases:
-            if id(c["M"]) in seen or (args.csr_kernel and c["fmt"] == "csr"):
+            if id(c["M"]) in seen or c["fmt"] in pinned:
                 continue
             seen.add(id(c["M"]))
             if c["fmt"] in ("sell", "sell_c_sigma", "sell_c_R", "csr5", "bsr"):
@@ -275,7 +282,7 @@ def run_gpu(args, rank, world):
                 "kernel": f"{dc['fam']}/{dc['fmt']}/{dc['dt']}",
                 "algorithmic_bytes": dc["bytes"]}
     cpu = None
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(hosts, families, dtypes, fmts, budget_s=15.0)
         log("cpu baseline done")
     for c in cases:
@@ -482,9 +489,11 @@ def run_serving():
     pinned-host and device buffers: saturation throughput and p50/p99 under
     Poisson load, batched vs one launch per request."""
     from sspmv_gb300 import serving
-    out = {}
+    model = ROOT / "sspmv_gb300" / "data" / "selector_model.npz"
+    out = {"selector_model": str(model.relative_to(ROOT)) if model.exists() else None}
     for kind, dev_buf in (("host", False), ("device", True)):
-        r = serving.serving_benchmark(64, device_buffers=dev_buf, log=log)
+        r = serving.serving_benchmark(64, device_buffers=dev_buf, log=log,
+                                      selector_model=model if model.exists() else None)
         out[kind] = r
     return out
 

@@ -229,10 +229,10 @@ sspmv_status sspmv_csr_export(const sspmv_csr *A, int32_t *row_offset, int32_t *
 sspmv_status sspmv_delete_csr(sspmv_csr *A);
 
 /* ---------------- SpMV / SpMM ---------------- */
-/* LeSpMV_csr (src/spmv_csr.cpp:165-185).  kernel_flag 0/2: nnz-balanced
- * merge-path kernel; 1: vector-per-row kernel; 3: nonzero-split stream
- * kernel (256 nonzeros per warp; matrices with runs of more than 256 empty
- * rows use merge-path). */
+/* LeSpMV_csr (src/spmv_csr.cpp:165-185).  kernel_flag 0 (default) / 3:
+ * nonzero-split stream kernel (256 nonzeros per warp; matrices with runs of
+ * more than 256 empty rows use merge-path); 2: nnz-balanced merge-path
+ * kernel; 1: vector-per-row kernel (param: lanes per row). */
 sspmv_status sspmv_LeSpMV_csr(double alpha, const sspmv_csr *A, const void *x, double beta, void *y,
                               sspmv_stream_t stream);
 sspmv_status sspmv_spmm_csr(double alpha, const sspmv_csr *A, int32_t k, const void *X, int64_t ldx,
@@ -272,7 +272,10 @@ sspmv_status sspmv_delete_ell(sspmv_ell *A);
  * 0 = reference defaults (4, 64/sizeof(value)). */
 sspmv_status sspmv_csr_to_sell(const sspmv_csr *csr, int32_t chunkwidth, int32_t alignment, sspmv_s_ell *out,
                                sspmv_stream_t stream);
-/* LeSpMV_sell (src/spmv_s_ell.cpp:203-224) */
+/* LeSpMV_sell (src/spmv_s_ell.cpp:203-224).  kernel_flag 0: a thread per
+ * row; 2 (chunkwidth < 32 dividing 32): a warp per 32 / C chunks reading
+ * each chunk's slab linearly.  The same flags apply to SELL-c-sigma and
+ * SELL-c-R. */
 sspmv_status sspmv_LeSpMV_sell(double alpha, const sspmv_s_ell *A, const void *x, double beta, void *y,
                                sspmv_stream_t stream);
 sspmv_status sspmv_spmm_sell(double alpha, const sspmv_s_ell *A, int32_t k, const void *X, int64_t ldx,

@@ -61,7 +61,9 @@ def tune_csr(M, x, y, reps: int = 10) -> dict:
 
 
 # Kernel candidates per format (formats with one kernel are not listed).
-KERNEL_CANDIDATES = {"csr": CSR_CANDIDATES, "coo": [(0, 0), (1, 0)]}
+SLICED_CANDIDATES = [(0, 0), (2, 0)]
+KERNEL_CANDIDATES = {"csr": CSR_CANDIDATES, "coo": [(0, 0), (1, 0)], "sell": SLICED_CANDIDATES,
+                     "sell_c_sigma": SLICED_CANDIDATES, "sell_c_R": SLICED_CANDIDATES}
 
 
 def conversion_candidates(fmt: str, num_rows: int) -> list[dict]:
@@ -111,7 +113,13 @@ def tune_conversion(csr, fmt: str, x, y, reps: int = 8, max_fill: float = 4.0):
             M.delete()
     if best is None:
         return None, None
-    return best[0], {"format": fmt, "params": best[2], "ms": best[1], "table": table}
+    M, ms, kw = best
+    rec = {"format": fmt, "params": kw, "ms": ms, "table": table}
+    if fmt in KERNEL_CANDIDATES:  # then the kernel for the chosen layout
+        k = tune_kernel(M, x, y, KERNEL_CANDIDATES[fmt], reps)
+        rec["kernel"] = k["best"]
+        rec["ms"] = min(ms, k["best"]["ms"])
+    return M, rec
 
 
 def tune_format(M, x, y, reps: int = 10) -> dict | None:

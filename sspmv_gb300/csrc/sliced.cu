@@ -94,6 +94,98 @@ __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
     }
 }
 
+// kernel_flag 2, C in {4, 8, 16}: a warp takes a group of G = 32 / C
+// consecutive chunks (32 rows) and reads the group's slabs as one linear
+// range, lane l on every 32nd slab element from l (row l % C of whichever
+// chunk the element falls in: chunk slabs are multiples of C long).  Each lane
+// keeps one partial sum per chunk of the group (chosen by comparing the
+// element's slab index with the group's chunk pointers, held in registers);
+// at the end the 32 / C partial sums of each row are added with shuffles.  A
+// thread per row keeps its warp busy for the longest of its 32 rows; here the
+// group costs its slab length, with 4 loads in flight per lane and no
+// per-chunk serialisation.  Padding (col -1) is read and skipped; chunks
+// wider than long_width are left to the pieces kernel.
+template <typename V, int K, int C>
+__global__ void __launch_bounds__(kBlock) sliced_group_kernel(
+    int m, int64_t nchunks, const int64_t *__restrict__ chunk_ptr, const int32_t *__restrict__ reorder,
+    const int32_t *__restrict__ col, const V *__restrict__ val, const V *__restrict__ x, int64_t ldx, V alpha,
+    V beta, V *__restrict__ y, int64_t ldy, int64_t long_width) {
+    constexpr int G = 32 / C;
+    constexpr unsigned kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int r = lane % C;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t c0 = warp * G; c0 < nchunks; c0 += nwarps * G) {  // warp-uniform
+        const int64_t mine = lane <= G ? ld_stream(chunk_ptr + min(c0 + lane, nchunks)) : 0;
+        int64_t ptr[G + 1];
+#pragma unroll
+        for (int t = 0; t <= G; t++) ptr[t] = __shfl_sync(kFull, mine, t);
+        unsigned longs = 0;  // chunks of the group handled by the pieces kernel
+#pragma unroll
+        for (int t = 0; t < G; t++)
+            if ((ptr[t + 1] - ptr[t]) / C > long_width) longs |= 1u << t;
+        V acc[G][K];
+#pragma unroll
+        for (int t = 0; t < G; t++)
+#pragma unroll
+            for (int q = 0; q < K; q++) acc[t][q] = V(0);
+        // runs of consecutive chunks the pieces kernel does not take (warp-uniform)
+        for (int ta = 0; ta < G;) {
+            if ((longs >> ta) & 1u) {
+                ta++;
+                continue;
+            }
+            int tb = ta + 1;
+            while (tb < G && !((longs >> tb) & 1u)) tb++;
+            const int64_t lo = __shfl_sync(kFull, mine, ta), hi = __shfl_sync(kFull, mine, tb);
+            for (int64_t e0 = lo + lane; e0 < hi; e0 += 4 * 32) {
+                int cc[4];
+                V aa[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int64_t e = e0 + 32 * u;
+                    cc[u] = e < hi ? ld_stream(col + e) : -1;
+                    aa[u] = e < hi ? ld_stream(val + e) : V(0);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    if (cc[u] < 0) continue;
+                    const int64_t e = e0 + 32 * u;
+                    int j = 0;  // chunk of the group holding slab element e
+#pragma unroll
+                    for (int t = 1; t < G; t++) j += e >= ptr[t];
+                    V prod[K];
+#pragma unroll
+                    for (int q = 0; q < K; q++) prod[q] = aa[u] * ld_x(x + (int64_t)cc[u] * ldx + q);
+#pragma unroll
+                    for (int t = 0; t < G; t++)
+                        if (t == j) {
+#pragma unroll
+                            for (int q = 0; q < K; q++) acc[t][q] += prod[q];
+                        }
+                }
+            }
+            ta = tb;
+        }
+#pragma unroll
+        for (int t = 0; t < G; t++) {
+#pragma unroll
+            for (int o = C; o < 32; o <<= 1)
+#pragma unroll
+                for (int q = 0; q < K; q++) acc[t][q] += __shfl_xor_sync(kFull, acc[t][q], o);
+            const int64_t c = c0 + t;
+            const int64_t i = c * C + r;
+            if (lane < C && c < nchunks && !((longs >> t) & 1u) && i < m) {
+                const int64_t row = reorder ? (int64_t)ld_stream(reorder + i) : i;
+                V *yp = y + row * ldy;
+#pragma unroll
+                for (int q = 0; q < K; q++) yp[q] = axpby(alpha, acc[t][q], beta, yp + q);
+            }
+        }
+    }
+}
+
 // piece = {chunk, first slot, end slot}; one warp per piece
 template <typename V, int K>
 __global__ void __launch_bounds__(kBlock) sliced_piece_kernel(
@@ -244,14 +336,34 @@ sspmv_status ensure_piece_plan(const sspmv_features *f, const SlicedView &v, Pla
     return SSPMV_OK;
 }
 
+// kernel_flag 2 with C in {4, 8, 16} and k <= 2: chunk-group kernel;
+// otherwise a thread per row.
 template <typename V, int K>
-sspmv_status launch_sliced(const SlicedView &v, Plan *p, V alpha, const V *x, int64_t ldx, V beta, V *y,
-                           int64_t ldy, sspmv_stream_t s) {
+sspmv_status launch_sliced(const SlicedView &v, Plan *p, int kernel_flag, V alpha, const V *x, int64_t ldx, V beta,
+                           V *y, int64_t ldy, sspmv_stream_t s) {
     const int64_t npieces = p ? p->extra_i[0] : 0;
-    const unsigned grid = grid_for(v.m, kBlock, (int64_t)num_sms() * 16);
-    sliced_spmv_kernel<V, K><<<grid, kBlock, 0, cu(s)>>>((int)v.m, v.C, v.chunk_ptr, v.reorder, v.col,
-                                                         (const V *)v.val, x, ldx, alpha, beta, y, ldy,
-                                                         npieces > 0 ? kLongWidth : INT64_MAX);
+    const int64_t long_width = npieces > 0 ? kLongWidth : INT64_MAX;
+    bool grouped = false;
+    if constexpr (K <= 2) {
+        if (kernel_flag == 2 && v.nchunks > 0 && (v.C == 4 || v.C == 8 || v.C == 16)) {
+            grouped = true;
+            const int64_t warps = (v.nchunks + (32 / v.C) - 1) / (32 / v.C);
+            const unsigned grid = grid_for(warps * 32, kBlock, (int64_t)num_sms() * 16);
+            auto go = [&](auto kern) {
+                kern<<<grid, kBlock, 0, cu(s)>>>((int)v.m, v.nchunks, v.chunk_ptr, v.reorder, v.col,
+                                                (const V *)v.val, x, ldx, alpha, beta, y, ldy, long_width);
+            };
+            if (v.C == 4) go(sliced_group_kernel<V, K, 4>);
+            else if (v.C == 8) go(sliced_group_kernel<V, K, 8>);
+            else go(sliced_group_kernel<V, K, 16>);
+        }
+    }
+    if (!grouped) {
+        const unsigned grid = grid_for(v.m, kBlock, (int64_t)num_sms() * 16);
+        sliced_spmv_kernel<V, K><<<grid, kBlock, 0, cu(s)>>>((int)v.m, v.C, v.chunk_ptr, v.reorder, v.col,
+                                                             (const V *)v.val, x, ldx, alpha, beta, y, ldy,
+                                                             long_width);
+    }
     SSPMV_LAUNCH_CHECK();
     if (npieces > 0) {
         const int64_t nlong = p->extra_i[1];
@@ -281,10 +393,10 @@ sspmv_status spmm_sliced(const sspmv_features *f, const SlicedView &v, double al
         return for_rhs_chunks<V>(k, (const V *)X, (V *)Y, [&](int32_t step, const V *xs, V *ys) {
             const V a = (V)alpha, b = (V)beta;
             switch (step) {
-            case 8: return launch_sliced<V, 8>(v, p, a, xs, ldx, b, ys, ldy, s);
-            case 4: return launch_sliced<V, 4>(v, p, a, xs, ldx, b, ys, ldy, s);
-            case 2: return launch_sliced<V, 2>(v, p, a, xs, ldx, b, ys, ldy, s);
-            default: return launch_sliced<V, 1>(v, p, a, xs, ldx, b, ys, ldy, s);
+            case 8: return launch_sliced<V, 8>(v, p, f->kernel_flag, a, xs, ldx, b, ys, ldy, s);
+            case 4: return launch_sliced<V, 4>(v, p, f->kernel_flag, a, xs, ldx, b, ys, ldy, s);
+            case 2: return launch_sliced<V, 2>(v, p, f->kernel_flag, a, xs, ldx, b, ys, ldy, s);
+            default: return launch_sliced<V, 1>(v, p, f->kernel_flag, a, xs, ldx, b, ys, ldy, s);
             }
         });
     });

@@ -226,7 +226,16 @@ class Dataset:
         return np.argmin(self.times, axis=1).astype(np.int32)
 
 
+PACKAGE_DATA = Path(__file__).resolve().parent / "data"
+
+
 def load_dataset(paths) -> Dataset:
+    """Labelled matrices from JSONL files written by build_dataset, or from
+    an .npz with raw / times / ids arrays (the packaged measured dataset,
+    sspmv_gb300/data/selector_dataset.npz)."""
+    if isinstance(paths, (str, Path)) and str(paths).endswith(".npz"):
+        d = np.load(paths)
+        return Dataset(np.asarray(d["raw"]), np.asarray(d["times"]), np.asarray(d["ids"]))
     recs = {}
     for p in ([paths] if isinstance(paths, (str, Path)) else paths):
         for ln in Path(p).read_text().splitlines():
@@ -524,10 +533,14 @@ def main(argv=None) -> None:
                 break
             build_dataset(a.out, min(step, a.start + a.count - s), s, a.seed, log)
         return
-    ds = load_dataset(a.data)
+    ds = load_dataset(a.data[0] if len(a.data) == 1 and a.data[0].endswith(".npz") else a.data)
     net, res = evaluate(ds, 0.8, a.seed, a.epochs, log)
     res["matrices"] = int(len(ds.ids))
-    save_model(net, a.model, common_params(a.data))
+    if a.data[0].endswith(".npz"):
+        params = json.loads(bytes(np.load(a.data[0])["format_params"]).decode())
+    else:
+        params = common_params(a.data)
+    save_model(net, a.model, params)
     Path(a.report).write_text(json.dumps(res, indent=1) + "\n")
     log(json.dumps(res))
 

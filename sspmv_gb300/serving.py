@@ -325,16 +325,19 @@ def select_formats(mats: list[dict], model_path, min_nnz: int = 1_000_000, log=N
 def serving_benchmark(num_matrices: int = 64, device_buffers: bool = False, duration_s: float = 1.5,
                       seed: int = 0, log=None, selector_model=None) -> dict:
     """Saturation throughput of the batched server and of per-request CSR
-    launches, then p50/p99 under Poisson load swept up to saturation.
-    'Equal p99' compares throughput at the per-request server's p99 at 70% of
-    its saturation rate."""
+    launches (8 requests in flight, and 1: the plain serial loop), then
+    p50/p99 under Poisson load swept up to saturation.  'Equal p99' takes a
+    baseline's most loaded sweep point and the batched server's best
+    throughput whose p99 is no higher."""
     log = log or (lambda *a: None)
     b = ServingBench(num_matrices, seed, device_buffers, log)
     picks = select_formats(b.mats, selector_model, log=log) if selector_model else None
     res = {"matrices": num_matrices, "registered": 2 * num_matrices, "total_nnz_per_precision": b.total_nnz,
            "buffers": "device" if device_buffers else "pinned host", "modes": {},
            "server_config": {"per_request": {"num_inflight": 8, "arena_bytes": 160 << 20},
-                             "batched": {"num_inflight": 3, "arena_bytes": 512 << 20}}}
+                             "per_request_serial": {"num_inflight": 1, "arena_bytes": 160 << 20},
+                             "batched": {"num_inflight": 4, "arena_bytes": 512 << 20,
+                                         "max_batch_tiles": 1 << 16}}}
     # Per-request launches get more requests in flight (they cannot batch).
     server_kw = res["server_config"]
     if picks:
@@ -343,15 +346,15 @@ def serving_benchmark(num_matrices: int = 64, device_buffers: bool = False, dura
     def fmt_of(mode):
         # the per-request comparison point is plain CSR; the batched server
         # serves each matrix in its selected format
-        if mode == "per_request" or not picks:
+        if mode != "batched" or not picks:
             return None
         return lambda mid, A: picks[mid // 2]
 
-    for mode in ("per_request", "batched"):
-        s = b.server(mode, fmt_of(mode), **server_kw[mode])
+    for mode in ("per_request_serial", "per_request", "batched"):
+        s = b.server("batched" if mode == "batched" else "per_request", fmt_of(mode), **server_kw[mode])
         try:
             b.run(s, 2000, 0.0, seed + 1)  # warm: graphs for the group sets, pools
-            sat = b.run(s, 20000 if mode == "batched" else 8000, 0.0, seed + 2)
+            sat = b.run(s, {"batched": 20000, "per_request": 8000, "per_request_serial": 3000}[mode], 0.0, seed + 2)
             log(f"[serving] {mode}: saturation {sat['req_per_s']:.0f} req/s, mean batch {sat['mean_batch']:.1f}")
             res["modes"][mode] = {"saturation": sat, "sweep": [], "stats": None}
             res["modes"][mode]["_server"] = s
@@ -359,9 +362,10 @@ def serving_benchmark(num_matrices: int = 64, device_buffers: bool = False, dura
             s.close()
             raise
     base = res["modes"]["per_request"]["saturation"]["req_per_s"]
-    fracs = {"per_request": (0.3, 0.5, 0.7, 0.9), "batched": (0.3, 0.7, 1.0, 1.5, 2.0, 3.0, 4.0, 6.0, 8.0)}
+    fracs = {"per_request_serial": (0.1, 0.2, 0.3), "per_request": (0.3, 0.5, 0.7, 0.9),
+             "batched": (0.3, 0.7, 1.0, 1.5, 2.0, 3.0, 4.0, 6.0, 8.0)}
     try:
-        for mode in ("per_request", "batched"):
+        for mode in ("per_request_serial", "per_request", "batched"):
             m = res["modes"][mode]
             satm = m["saturation"]["req_per_s"]
             for f in fracs[mode]:
@@ -378,12 +382,21 @@ def serving_benchmark(num_matrices: int = 64, device_buffers: bool = False, dura
     finally:
         for mode in res["modes"].values():
             mode.pop("_server").close()
-    pr = [r for r in res["modes"]["per_request"]["sweep"] if r["fraction_of_per_request_saturation"] == 0.7]
-    if pr:
-        target = pr[0]["p99_us"]
+    # throughput at equal p99: the baseline's most loaded sweep point whose
+    # p99 is the target, against the batched server's best throughput within it
+    res["saturation_ratio"] = {m: res["modes"]["batched"]["saturation"]["req_per_s"] /
+                               max(res["modes"][m]["saturation"]["req_per_s"], 1e-9)
+                               for m in ("per_request", "per_request_serial")}
+    res["equal_p99"] = {}
+    for base_mode in ("per_request", "per_request_serial"):
+        sw = res["modes"][base_mode]["sweep"]
+        if not sw:
+            continue
+        ref = sw[-1]
+        target = ref["p99_us"]
         ok = [r for r in res["modes"]["batched"]["sweep"] if r["p99_us"] is not None and r["p99_us"] <= target]
         best = max((r["req_per_s"] for r in ok), default=None)
-        res["equal_p99"] = {"p99_target_us": target, "per_request_req_per_s": pr[0]["req_per_s"],
-                            "batched_req_per_s": best,
-                            "throughput_ratio": (best / pr[0]["req_per_s"]) if best else None}
+        res["equal_p99"][base_mode] = {"p99_target_us": target, "baseline_req_per_s": ref["req_per_s"],
+                                       "batched_req_per_s": best,
+                                       "throughput_ratio": (best / ref["req_per_s"]) if best else None}
     return res

@@ -115,7 +115,17 @@ ORACLE_CONV = {
     "csr5": lambda O, A: O.csr_to_csr5(A),
     "csr5_w32": lambda O, A: O.csr_to_csr5(A, 16, 32),
     "csr5_s12_w4": lambda O, A: O.csr_to_csr5(A, 12, 4),
+    "sell_c4_warp": lambda O, A: O.csr_to_sell(A, 4, 4),
+    "scs_c8_warp": lambda O, A: O.csr_to_sell_c_sigma(A, 256, 8, 1),
+    "scr_c16_warp": lambda O, A: O.csr_to_sell_c_R(A, 16),
 }
+
+
+def _kernel(M, flag):
+    M.set_kernel(flag, 0)
+    return M
+
+
 GPU_CONV = {
     "ell": lambda L, M: L.csr_to_ell(M, 0),
     "sell": lambda L, M: L.csr_to_sell(M, 8, 4),
@@ -129,6 +139,10 @@ GPU_CONV = {
     "csr5": lambda L, M: L.csr_to_csr5(M),
     "csr5_w32": lambda L, M: L.csr_to_csr5(M, 16, 32),
     "csr5_s12_w4": lambda L, M: L.csr_to_csr5(M, 12, 4),
+    # the warp-per-chunk-group sliced kernel (kernel_flag 2)
+    "sell_c4_warp": lambda L, M: _kernel(L.csr_to_sell(M, 4, 4), 2),
+    "scs_c8_warp": lambda L, M: _kernel(L.csr_to_sell_c_sigma(M, 256, 8, 1), 2),
+    "scr_c16_warp": lambda L, M: _kernel(L.csr_to_sell_c_R(M, 16), 2),
 }
 
 

@@ -119,3 +119,17 @@ def test_label_matrix_times_every_feasible_format():
     assert len(rec["raw"]) == 66 and rec["raw"][43] == 5
     for f in ("csr", "coo", "ell", "sell", "sell_c_sigma", "sell_c_R", "dia", "csr5"):
         assert rec["times"][f] is not None and rec["times"][f] > 0, f
+
+
+def test_packaged_selector_regret_on_held_out_matrices():
+    """The packaged model (trained on the first 1,600 of the packaged 2,000
+    GPU-labelled matrices, seed-0 split) picks formats on the other 400 with
+    far lower regret than always using CSR."""
+    from sspmv_gb300 import selector as S
+    ds = S.load_dataset(S.PACKAGE_DATA / "selector_dataset.npz")
+    perm = np.random.default_rng(0).permutation(len(ds.ids))
+    te = perm[1600:]
+    net = S.load_model(S.PACKAGE_DATA / "selector_model.npz")
+    picks = S.choose(net, ds.raw[te], np.isfinite(ds.times[te]))
+    r = S.regret(ds.times[te], picks)
+    assert r["mean_regret"] < 0.05 and r["mean_regret"] < r["csr_mean_regret"] / 3, r

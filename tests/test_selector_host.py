@@ -79,3 +79,13 @@ def test_feasibility_from_features_and_server_params():
     assert server_params("sell_c_sigma", {"slicewidth": 256, "chunkwidth": 8, "alignment": 0}) == [256, 8, 0]
     assert server_params("bsr", {"blockDimRow": 2, "blockDimCol": 4}) == [2, 4]
     assert server_params("csr", {"kernel_flag": 1, "param": 4}) is None
+
+
+def test_packaged_dataset_is_consistent():
+    from sspmv_gb300 import selector as S
+    ds = S.load_dataset(S.PACKAGE_DATA / "selector_dataset.npz")
+    assert ds.raw.shape == (2000, 66) and ds.times.shape == (2000, 9)
+    assert np.isfinite(ds.times[:, S.CSR_LABEL]).all() and (ds.times > 0).all()
+    assert set(np.unique(ds.labels)) <= set(range(S.NUM_CLASSES))
+    hist = np.bincount(ds.labels, minlength=S.NUM_CLASSES)
+    assert hist[S.CSR_LABEL] < 0.6 * len(ds.ids)  # CSR is often, not always, fastest
