@@ -644,11 +644,14 @@ def _barrier(world):
 
 
 def _max_over_ranks(v, world):
+    """Max of v over the ranks (NCCL on the GPUs; gloo process groups, as in
+    the CPU tests, reduce on the host)."""
     if world == 1:
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 

@@ -272,10 +272,7 @@ sspmv_status sspmv_delete_ell(sspmv_ell *A);
  * 0 = reference defaults (4, 64/sizeof(value)). */
 sspmv_status sspmv_csr_to_sell(const sspmv_csr *csr, int32_t chunkwidth, int32_t alignment, sspmv_s_ell *out,
                                sspmv_stream_t stream);
-/* LeSpMV_sell (src/spmv_s_ell.cpp:203-224).  kernel_flag 0: a thread per
- * row; 2 (chunkwidth < 32 dividing 32): a warp per 32 / C chunks reading
- * each chunk's slab linearly.  The same flags apply to SELL-c-sigma and
- * SELL-c-R. */
+/* LeSpMV_sell (src/spmv_s_ell.cpp:203-224) */
 sspmv_status sspmv_LeSpMV_sell(double alpha, const sspmv_s_ell *A, const void *x, double beta, void *y,
                                sspmv_stream_t stream);
 sspmv_status sspmv_spmm_sell(double alpha, const sspmv_s_ell *A, int32_t k, const void *X, int64_t ldx,

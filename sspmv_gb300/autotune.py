@@ -61,9 +61,7 @@ def tune_csr(M, x, y, reps: int = 10) -> dict:
 
 
 # Kernel candidates per format (formats with one kernel are not listed).
-SLICED_CANDIDATES = [(0, 0), (2, 0)]
-KERNEL_CANDIDATES = {"csr": CSR_CANDIDATES, "coo": [(0, 0), (1, 0)], "sell": SLICED_CANDIDATES,
-                     "sell_c_sigma": SLICED_CANDIDATES, "sell_c_R": SLICED_CANDIDATES}
+KERNEL_CANDIDATES = {"csr": CSR_CANDIDATES, "coo": [(0, 0), (1, 0)]}
 
 
 def conversion_candidates(fmt: str, num_rows: int) -> list[dict]:
@@ -144,3 +142,63 @@ def load_log(path: str | Path) -> dict:
                 rec = json.loads(line)
                 out[rec["key"]] = rec
     return out
+
+
+def kernel_table(families, dtypes=("f64", "f32"), ks=(1, 2, 4, 8), flags=((0, 0), (2, 0), (1, 0)), reps: int = 5,
+                 log=None) -> list[dict]:
+    """Times the CSR kernels (stream, merge-path, vector) on the named
+    synthetic workloads for k right-hand sides; one record per (workload,
+    precision, k, kernel): median ms (L2 flushed), algorithmic GB/s."""
+    import numpy as np
+    import torch
+    from . import synth
+    flush = torch.empty(L2_FLUSH // 4, dtype=torch.float32, device="cuda")
+    out = []
+    for fam in families:
+        for dt in dtypes:
+            dtype = np.float64 if dt == "f64" else np.float32
+            A = synth.load(fam, 1, dtype)
+            csr = L.csr_from_host(A)
+            for k in ks:
+                X = torch.from_numpy(synth.vector(A.num_cols, 0, dtype, k).reshape(A.num_cols, k)).cuda()
+                Y = torch.zeros((A.num_rows, k), dtype=X.dtype, device="cuda")
+                for flag, param in flags:
+                    csr.set_kernel(flag, param)
+                    ts = []
+                    for i in range(reps + 1):
+                        flush.zero_()
+                        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                        e0.record()
+                        L.spmm(1.0, csr, X, 0.0, Y)
+                        e1.record()
+                        e1.synchronize()
+                        if i:
+                            ts.append(e0.elapsed_time(e1))
+                    ms = sorted(ts)[len(ts) // 2]
+                    rec = {"workload": fam, "dtype": dt, "k": k, "kernel_flag": flag, "param": param,
+                           "ms": round(ms, 4), "GBps": round(csr.algorithmic_bytes(k, False) / ms / 1e6, 1)}
+                    out.append(rec)
+                    if log:
+                        log(json.dumps(rec))
+            csr.delete()
+    return out
+
+
+def main(argv=None) -> None:
+    """python -m sspmv_gb300.autotune table --families powerlaw_4M,uniform_4M [--ks 1,2,4,8]"""
+    import argparse
+    import sys
+    ap = argparse.ArgumentParser(prog="python -m sspmv_gb300.autotune")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    t = sub.add_parser("table", help="CSR kernels x k right-hand sides on synthetic workloads")
+    t.add_argument("--families", default="powerlaw_4M,uniform_4M,banded_2M,block4_2M")
+    t.add_argument("--dtypes", default="f64,f32")
+    t.add_argument("--ks", default="1,2,4,8")
+    a = ap.parse_args(argv)
+    kernel_table(a.families.split(","), a.dtypes.split(","), [int(k) for k in a.ks.split(",")],
+                 log=lambda s: print(s, flush=True))
+    sys.stdout.flush()
+
+
+if __name__ == "__main__":
+    main()

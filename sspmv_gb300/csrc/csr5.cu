@@ -267,11 +267,14 @@ __global__ void __launch_bounds__(kBlock) csr5_tile_kernel(C5View A, const V *__
     int32_t rel = yoff;
     const uint32_t bit0 = active ? c5_bit<OMEGA>(dl, xl, 0, A.bao, d0) : 0u;
     if (active) {
-        for (int i0 = 0; i0 < sigma; i0 += 4) {
-            int cc[4];
-            V aa[4];
+        // nonzeros whose loads (and x gathers) are in flight together: 8 for
+        // f32 at k = 1; 4 otherwise (deeper prefetch measured slower for f64)
+        constexpr int kU = (sizeof(V) == 4 && K == 1) ? 8 : 4;
+        for (int i0 = 0; i0 < sigma; i0 += kU) {
+            int cc[kU];
+            V aa[kU], xv[kU][K];
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
+            for (int u = 0; u < kU; u++) {
                 const int i = i0 + u;
                 cc[u] = 0;
                 aa[u] = V(0);
@@ -282,7 +285,11 @@ __global__ void __launch_bounds__(kBlock) csr5_tile_kernel(C5View A, const V *__
                 }
             }
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
+            for (int u = 0; u < kU; u++)
+#pragma unroll
+                for (int q = 0; q < K; q++) xv[u][q] = i0 + u < sigma ? ld_x(x + (int64_t)cc[u] * ldx + q) : V(0);
+#pragma unroll
+            for (int u = 0; u < kU; u++) {
                 const int i = i0 + u;
                 if (i >= sigma) break;
                 const uint32_t b = (xl == 0 && i == 0) ? 0u : (i == 0 ? bit0 : c5_bit<OMEGA>(dl, xl, i, A.bao, d0));
@@ -300,9 +307,8 @@ __global__ void __launch_bounds__(kBlock) csr5_tile_kernel(C5View A, const V *__
 #pragma unroll
                     for (int q = 0; q < K; q++) sum[q] = V(0);
                 }
-                const V *xp = x + (int64_t)cc[u] * ldx;
 #pragma unroll
-                for (int q = 0; q < K; q++) sum[q] += aa[u] * ld_x(xp + q);
+                for (int q = 0; q < K; q++) sum[q] += aa[u] * xv[u][q];
             }
         }
     }

@@ -38,10 +38,15 @@ namespace {
 constexpr int kBlock = 256;
 
 // ------------------------------------------------------------------ SpMV --
-// Chunks wider than kLongWidth slots are not handled a thread per row (a
-// 38k-slot row would serialise its warp): they are cut into pieces of about
-// kPieceElems slab elements, each read by one warp with consecutive lanes on
-// consecutive slab elements, and a fix-up adds a chunk's pieces in order.
+// A thread per stored row reads its slots (C consecutive rows read together)
+// up to its first padding slot.  In chunks wider than kLongWidth slots only
+// the first kLongWidth are read this way (a 38k-slot row would serialise its
+// warp): the slots past them of each row that goes on (the "overflow", found
+// once per matrix) are copied into compact arrays when the plan is built,
+// summed there in pieces of about kPieceElems nonzeros, one warp each, and a
+// fix-up adds a row's thread partial and its pieces in order.  The compact
+// copy reads only the long rows' nonzeros, not the padding of the short rows
+// sharing their chunks (slot-major storage puts them in the same sectors).
 constexpr int64_t kLongWidth = 64;
 constexpr int64_t kPieceElems = 2048;
 
@@ -49,13 +54,14 @@ template <typename V, int K>
 __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
     int m, int C, const int64_t *__restrict__ chunk_ptr, const int32_t *__restrict__ reorder,
     const int32_t *__restrict__ col, const V *__restrict__ val, const V *__restrict__ x, int64_t ldx, V alpha,
-    V beta, V *__restrict__ y, int64_t ldy, int64_t long_width) {
+    V beta, V *__restrict__ y, int64_t ldy, int64_t long_width, const int32_t *__restrict__ ovf_id,
+    V *__restrict__ ovf_part) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t c = i / C;
         const int r = (int)(i - c * C);
         const int64_t base = ld_stream(chunk_ptr + c);
-        const int64_t w = (ld_stream(chunk_ptr + c + 1) - base) / C;
-        if (w > long_width) continue;  // pieces kernel
+        const int64_t wfull = (ld_stream(chunk_ptr + c + 1) - base) / C;
+        const int64_t w = min(wfull, long_width);
         const int32_t *cp = col + base + r;
         const V *vp = val + base + r;
         V s[K];
@@ -87,6 +93,12 @@ __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
                 for (int q = 0; q < K; q++) s[q] += aa * ld_x(x + (int64_t)cc * ldx + q);
             }
         }
+        if (wfull > w && ld_stream(cp + w * C) >= 0) {  // the row goes on: overflow
+            V *op = ovf_part + (int64_t)ovf_id[i] * kMaxK;
+#pragma unroll
+            for (int q = 0; q < K; q++) op[q] = s[q];
+            continue;
+        }
         const int64_t row = reorder ? (int64_t)ld_stream(reorder + i) : i;
         V *yp = y + row * ldy;
 #pragma unroll
@@ -94,190 +106,115 @@ __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
     }
 }
 
-// kernel_flag 2, C in {4, 8, 16}: a warp takes a group of G = 32 / C
-// consecutive chunks (32 rows) and reads the group's slabs as one linear
-// range, lane l on every 32nd slab element from l (row l % C of whichever
-// chunk the element falls in: chunk slabs are multiples of C long).  Each lane
-// keeps one partial sum per chunk of the group (chosen by comparing the
-// element's slab index with the group's chunk pointers, held in registers);
-// at the end the 32 / C partial sums of each row are added with shuffles.  A
-// thread per row keeps its warp busy for the longest of its 32 rows; here the
-// group costs its slab length, with 4 loads in flight per lane and no
-// per-chunk serialisation.  Padding (col -1) is read and skipped; chunks
-// wider than long_width are left to the pieces kernel.
-template <typename V, int K, int C>
-__global__ void __launch_bounds__(kBlock) sliced_group_kernel(
-    int m, int64_t nchunks, const int64_t *__restrict__ chunk_ptr, const int32_t *__restrict__ reorder,
-    const int32_t *__restrict__ col, const V *__restrict__ val, const V *__restrict__ x, int64_t ldx, V alpha,
-    V beta, V *__restrict__ y, int64_t ldy, int64_t long_width) {
-    constexpr int G = 32 / C;
-    constexpr unsigned kFull = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const int r = lane % C;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t c0 = warp * G; c0 < nchunks; c0 += nwarps * G) {  // warp-uniform
-        const int64_t mine = lane <= G ? ld_stream(chunk_ptr + min(c0 + lane, nchunks)) : 0;
-        int64_t ptr[G + 1];
-#pragma unroll
-        for (int t = 0; t <= G; t++) ptr[t] = __shfl_sync(kFull, mine, t);
-        unsigned longs = 0;  // chunks of the group handled by the pieces kernel
-#pragma unroll
-        for (int t = 0; t < G; t++)
-            if ((ptr[t + 1] - ptr[t]) / C > long_width) longs |= 1u << t;
-        V acc[G][K];
-#pragma unroll
-        for (int t = 0; t < G; t++)
-#pragma unroll
-            for (int q = 0; q < K; q++) acc[t][q] = V(0);
-        // runs of consecutive chunks the pieces kernel does not take (warp-uniform)
-        for (int ta = 0; ta < G;) {
-            if ((longs >> ta) & 1u) {
-                ta++;
-                continue;
-            }
-            int tb = ta + 1;
-            while (tb < G && !((longs >> tb) & 1u)) tb++;
-            const int64_t lo = __shfl_sync(kFull, mine, ta), hi = __shfl_sync(kFull, mine, tb);
-            for (int64_t e0 = lo + lane; e0 < hi; e0 += 4 * 32) {
-                int cc[4];
-                V aa[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const int64_t e = e0 + 32 * u;
-                    cc[u] = e < hi ? ld_stream(col + e) : -1;
-                    aa[u] = e < hi ? ld_stream(val + e) : V(0);
-                }
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    if (cc[u] < 0) continue;
-                    const int64_t e = e0 + 32 * u;
-                    int j = 0;  // chunk of the group holding slab element e
-#pragma unroll
-                    for (int t = 1; t < G; t++) j += e >= ptr[t];
-                    V prod[K];
-#pragma unroll
-                    for (int q = 0; q < K; q++) prod[q] = aa[u] * ld_x(x + (int64_t)cc[u] * ldx + q);
-#pragma unroll
-                    for (int t = 0; t < G; t++)
-                        if (t == j) {
-#pragma unroll
-                            for (int q = 0; q < K; q++) acc[t][q] += prod[q];
-                        }
-                }
-            }
-            ta = tb;
-        }
-#pragma unroll
-        for (int t = 0; t < G; t++) {
-#pragma unroll
-            for (int o = C; o < 32; o <<= 1)
-#pragma unroll
-                for (int q = 0; q < K; q++) acc[t][q] += __shfl_xor_sync(kFull, acc[t][q], o);
-            const int64_t c = c0 + t;
-            const int64_t i = c * C + r;
-            if (lane < C && c < nchunks && !((longs >> t) & 1u) && i < m) {
-                const int64_t row = reorder ? (int64_t)ld_stream(reorder + i) : i;
-                V *yp = y + row * ldy;
-#pragma unroll
-                for (int q = 0; q < K; q++) yp[q] = axpby(alpha, acc[t][q], beta, yp + q);
-            }
-        }
-    }
-}
-
-// piece = {chunk, first slot, end slot}; one warp per piece
+// piece = {overflow row, first element, end element} of the compact arrays;
+// one warp per piece, lanes on consecutive elements
 template <typename V, int K>
-__global__ void __launch_bounds__(kBlock) sliced_piece_kernel(
-    int64_t npieces, int C, const int4 *__restrict__ pieces, const int64_t *__restrict__ chunk_ptr,
-    const int32_t *__restrict__ col, const V *__restrict__ val, const V *__restrict__ x, int64_t ldx,
-    V *__restrict__ partial) {
+__global__ void __launch_bounds__(kBlock) sliced_piece_kernel(int64_t npieces, const int4 *__restrict__ pieces,
+                                                              const int32_t *__restrict__ ocol,
+                                                              const V *__restrict__ oval, const V *__restrict__ x,
+                                                              int64_t ldx, V *__restrict__ partial) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (warp >= npieces) return;
     const int4 pc = pieces[warp];
-    const int64_t base = chunk_ptr[pc.x];
-    V *out = partial + warp * (int64_t)C * kMaxK;
-    if (32 % C == 0) {
-        // lane -> (row lane % C, slot lane / C): a warp step reads 32
-        // consecutive slab elements
-        const int r = lane % C, sl = lane / C, step = 32 / C;
-        V s[K];
-#pragma unroll
-        for (int q = 0; q < K; q++) s[q] = V(0);
-        int64_t k = pc.y + sl;
-        for (; k + 3 * step < pc.z; k += 4 * step) {
-            int cc[4];
-            V aa[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const int64_t idx = base + (k + u * step) * C + r;
-                cc[u] = ld_stream(col + idx);
-                aa[u] = ld_stream(val + idx);
-            }
-#pragma unroll
-            for (int u = 0; u < 4; u++)
-                if (cc[u] >= 0) {
-#pragma unroll
-                    for (int q = 0; q < K; q++) s[q] += aa[u] * ld_x(x + (int64_t)cc[u] * ldx + q);
-                }
-        }
-        for (; k < pc.z; k += step) {
-            const int64_t idx = base + k * C + r;
-            const int cc = ld_stream(col + idx);
-            if (cc >= 0) {
-                const V aa = ld_stream(val + idx);
-#pragma unroll
-                for (int q = 0; q < K; q++) s[q] += aa * ld_x(x + (int64_t)cc * ldx + q);
-            }
-        }
-        for (int o = C; o < 32; o <<= 1)
-#pragma unroll
-            for (int q = 0; q < K; q++) s[q] += __shfl_xor_sync(0xffffffffu, s[q], o);
-        if (lane < C) {
-#pragma unroll
-            for (int q = 0; q < K; q++) out[r * kMaxK + q] = s[q];
-        }
-    } else {
-        for (int r = lane; r < C; r += 32) {  // rows of the chunk, one lane each
-            V s[K];
-#pragma unroll
-            for (int q = 0; q < K; q++) s[q] = V(0);
-            for (int64_t k = pc.y; k < pc.z; k++) {
-                const int64_t idx = base + k * C + r;
-                const int cc = ld_stream(col + idx);
-                if (cc < 0) break;
-                const V aa = ld_stream(val + idx);
-#pragma unroll
-                for (int q = 0; q < K; q++) s[q] += aa * ld_x(x + (int64_t)cc * ldx + q);
-            }
-#pragma unroll
-            for (int q = 0; q < K; q++) out[r * kMaxK + q] = s[q];
-        }
-    }
-}
-
-// one thread per (long chunk, row): adds the chunk's pieces in order
-template <typename V, int K>
-__global__ void sliced_piece_fixup(int64_t nlong, int64_t m, int C, const int32_t *__restrict__ long_chunks,
-                                   const int32_t *__restrict__ piece_begin, const int32_t *__restrict__ reorder,
-                                   const V *__restrict__ partial, V alpha, V beta, V *__restrict__ y, int64_t ldy) {
-    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid >= nlong * C) return;
-    const int64_t L = tid / C;
-    const int r = (int)(tid - L * C);
-    const int64_t i = (int64_t)long_chunks[L] * C + r;
-    if (i >= m) return;
     V s[K];
 #pragma unroll
     for (int q = 0; q < K; q++) s[q] = V(0);
-    for (int32_t p = piece_begin[L]; p < piece_begin[L + 1]; p++)
+    int64_t e = (int64_t)pc.y + lane;
+    for (; e + 96 < pc.z; e += 128) {
+        int cc[4];
+        V aa[4];
 #pragma unroll
-        for (int q = 0; q < K; q++) s[q] += partial[((int64_t)p * C + r) * kMaxK + q];
+        for (int u = 0; u < 4; u++) {
+            cc[u] = ld_stream(ocol + e + 32 * u);
+            aa[u] = ld_stream(oval + e + 32 * u);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int q = 0; q < K; q++) s[q] += aa[u] * ld_x(x + (int64_t)cc[u] * ldx + q);
+    }
+    for (; e < pc.z; e += 32) {
+        const int cc = ld_stream(ocol + e);
+        const V aa = ld_stream(oval + e);
+#pragma unroll
+        for (int q = 0; q < K; q++) s[q] += aa * ld_x(x + (int64_t)cc * ldx + q);
+    }
+#pragma unroll
+    for (int q = 0; q < K; q++) s[q] = warp_sum(s[q]);
+    if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < K; q++) partial[warp * kMaxK + q] = s[q];
+    }
+}
+
+// one thread per overflow row: its thread partial plus its pieces, in order
+template <typename V, int K>
+__global__ void sliced_piece_fixup(int64_t nov, const int32_t *__restrict__ ovf_rows,
+                                   const int32_t *__restrict__ piece_begin, const int32_t *__restrict__ reorder,
+                                   const V *__restrict__ ovf_part, const V *__restrict__ partial, V alpha, V beta,
+                                   V *__restrict__ y, int64_t ldy) {
+    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= nov) return;
+    V s[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) s[q] = ovf_part[o * kMaxK + q];
+    for (int32_t p = piece_begin[o]; p < piece_begin[o + 1]; p++)
+#pragma unroll
+        for (int q = 0; q < K; q++) s[q] += partial[(int64_t)p * kMaxK + q];
+    const int64_t i = ovf_rows[o];
     const int64_t row = reorder ? (int64_t)reorder[i] : i;
     V *yp = y + row * ldy;
 #pragma unroll
     for (int q = 0; q < K; q++) yp[q] = axpby(alpha, s[q], beta, yp + q);
+}
+
+// Plan building: stored length of each row of a long chunk (padding is a
+// suffix: binary search for the first slot with col < 0).
+__global__ void long_row_lengths(int64_t ncand, int C, const int32_t *__restrict__ cand,
+                                 const int64_t *__restrict__ chunk_ptr, const int32_t *__restrict__ col,
+                                 int32_t *__restrict__ len) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncand) return;
+    const int64_t i = cand[t];
+    const int64_t c = i / C;
+    const int r = (int)(i - c * C);
+    const int64_t base = chunk_ptr[c];
+    const int64_t w = (chunk_ptr[c + 1] - base) / C;
+    int64_t lo = 0, hi = w;  // first padding slot in [0, w]
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (col[base + mid * C + r] >= 0) lo = mid + 1;
+        else hi = mid;
+    }
+    len[t] = (int32_t)lo;
+}
+
+// Overflow ids of the stored rows: ovf_id[rows[o]] = o.
+__global__ void set_overflow_ids(int64_t nov, const int32_t *__restrict__ rows, int32_t *__restrict__ ovf_id) {
+    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o < nov) ovf_id[rows[o]] = (int32_t)o;
+}
+
+// Copies slots kLongWidth.. of each overflow row into the compact arrays
+// (one warp per row).
+template <typename V>
+__global__ void copy_overflow(int64_t nov, int C, const int32_t *__restrict__ ovf_rows,
+                              const int64_t *__restrict__ ovf_ptr, const int64_t *__restrict__ chunk_ptr,
+                              const int32_t *__restrict__ col, const V *__restrict__ val, int32_t *__restrict__ ocol,
+                              V *__restrict__ oval) {
+    const int lane = threadIdx.x & 31;
+    const int64_t o = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (o >= nov) return;
+    const int64_t i = ovf_rows[o];
+    const int64_t c = i / C;
+    const int r = (int)(i - c * C);
+    const int64_t base = chunk_ptr[c] + kLongWidth * C + r;
+    const int64_t n = ovf_ptr[o + 1] - ovf_ptr[o], dst = ovf_ptr[o];
+    for (int64_t e = lane; e < n; e += 32) {
+        ocol[dst + e] = col[base + e * C];
+        oval[dst + e] = val[base + e * C];
+    }
 }
 
 struct SlicedView {
@@ -290,10 +227,12 @@ struct SlicedView {
     int64_t nchunks;
 };
 
-// Piece plan of a sliced matrix, built on its first SpMV from the chunk
-// widths: extra[0] pieces (int4), extra[1] long chunk ids, extra[2] first
-// piece of each long chunk (+1 entry), extra[3] partial sums;
-// extra_i[0] pieces, extra_i[1] long chunks.
+// Overflow plan of a sliced matrix, built on its first SpMV: extra[0]
+// pieces (int4), extra[1] overflow rows (stored row positions), extra[2]
+// first piece of each overflow row (+1 entry), extra[3] piece partials,
+// extra[4] thread partials of the overflow rows, extra[5] / extra[6] compact
+// columns / values, extra[8] overflow id per stored row (-1: none);
+// extra_i[0] pieces, extra_i[1] overflow rows, extra_i[7] built.
 sspmv_status ensure_piece_plan(const sspmv_features *f, const SlicedView &v, Plan *p, sspmv_stream_t s) {
     if (p->extra_i[7]) return SSPMV_OK;
     std::lock_guard<std::mutex> g(plan_mutex());
@@ -301,77 +240,106 @@ sspmv_status ensure_piece_plan(const sspmv_features *f, const SlicedView &v, Pla
     std::vector<int64_t> cp((size_t)v.nchunks + 1);
     SSPMV_CUDA_TRY(cudaMemcpyAsync(cp.data(), v.chunk_ptr, cp.size() * 8, cudaMemcpyDeviceToHost, cu(s)));
     SSPMV_CUDA_TRY(cudaStreamSynchronize(cu(s)));
-    const int64_t piece_w = std::max<int64_t>(kLongWidth, kPieceElems / std::max<int32_t>(v.C, 1));
-    std::vector<int4> pieces;
-    std::vector<int32_t> longs, begin;
+    std::vector<int32_t> cand;  // stored rows of long chunks
     for (int64_t c = 0; c < v.nchunks; c++) {
         const int64_t w = (cp[(size_t)c + 1] - cp[(size_t)c]) / v.C;
         if (w <= kLongWidth) continue;
-        longs.push_back((int32_t)c);
-        begin.push_back((int32_t)pieces.size());
-        for (int64_t k0 = 0; k0 < w; k0 += piece_w)
-            pieces.push_back(make_int4((int)c, (int)k0, (int)std::min(w, k0 + piece_w), 0));
+        for (int r = 0; r < v.C && c * v.C + r < v.m; r++) cand.push_back((int32_t)(c * v.C + r));
     }
-    begin.push_back((int32_t)pieces.size());
-    if (!pieces.empty()) {
-        int4 *dp = nullptr;
-        int32_t *dl = nullptr, *db = nullptr;
-        unsigned char *part = nullptr;
-        SSPMV_TRY(dalloc(&dp, pieces.size(), s));
-        SSPMV_TRY(dalloc(&dl, longs.size(), s));
-        SSPMV_TRY(dalloc(&db, begin.size(), s));
-        SSPMV_TRY(dalloc(&part, pieces.size() * (size_t)v.C * kMaxK * vsize(f->value_type), s));
-        SSPMV_CUDA_TRY(cudaMemcpyAsync(dp, pieces.data(), pieces.size() * sizeof(int4), cudaMemcpyHostToDevice, cu(s)));
-        SSPMV_CUDA_TRY(cudaMemcpyAsync(dl, longs.data(), longs.size() * 4, cudaMemcpyHostToDevice, cu(s)));
-        SSPMV_CUDA_TRY(cudaMemcpyAsync(db, begin.data(), begin.size() * 4, cudaMemcpyHostToDevice, cu(s)));
+    if (!cand.empty()) {
+        const size_t sv = vsize(f->value_type);
+        int32_t *dcand = nullptr, *dlen = nullptr;
+        SSPMV_TRY(dalloc(&dcand, cand.size(), s));
+        SSPMV_TRY(dalloc(&dlen, cand.size(), s));
+        SSPMV_CUDA_TRY(cudaMemcpyAsync(dcand, cand.data(), cand.size() * 4, cudaMemcpyHostToDevice, cu(s)));
+        long_row_lengths<<<grid_for((int64_t)cand.size(), 256), 256, 0, cu(s)>>>((int64_t)cand.size(), v.C, dcand,
+                                                                                v.chunk_ptr, v.col, dlen);
+        SSPMV_LAUNCH_CHECK();
+        std::vector<int32_t> len(cand.size());
+        SSPMV_CUDA_TRY(cudaMemcpyAsync(len.data(), dlen, len.size() * 4, cudaMemcpyDeviceToHost, cu(s)));
         SSPMV_CUDA_TRY(cudaStreamSynchronize(cu(s)));
-        p->extra[0] = dp;
-        p->extra[1] = dl;
-        p->extra[2] = db;
-        p->extra[3] = part;
-        p->extra_i[0] = (int64_t)pieces.size();
-        p->extra_i[1] = (int64_t)longs.size();
+        dfree(dcand, s);
+        dfree(dlen, s);
+        std::vector<int32_t> rows, begin;
+        std::vector<int64_t> optr{0};
+        std::vector<int4> pieces;
+        for (size_t t = 0; t < cand.size(); t++) {
+            if (len[t] <= kLongWidth) continue;
+            const int64_t n = len[t] - kLongWidth, o0 = optr.back();
+            if (o0 + n > 0x7fffffff) return fail(SSPMV_NOT_SUPPORTED, "long-row overflow exceeds the int32 range");
+            rows.push_back(cand[t]);
+            begin.push_back((int32_t)pieces.size());
+            for (int64_t e = 0; e < n; e += kPieceElems)
+                pieces.push_back(make_int4((int)rows.size() - 1, (int)(o0 + e), (int)(o0 + std::min(n, e + kPieceElems)),
+                                           0));
+            optr.push_back(o0 + n);
+        }
+        begin.push_back((int32_t)pieces.size());
+        const int64_t nov = (int64_t)rows.size(), novf = optr.back();
+        if (nov > 0) {
+            int4 *dp = nullptr;
+            int32_t *drows = nullptr, *db = nullptr, *dov = nullptr, *ocol = nullptr;
+            int64_t *dptr = nullptr;
+            unsigned char *part = nullptr, *opart = nullptr, *oval = nullptr;
+            SSPMV_TRY(dalloc(&dp, pieces.size(), s));
+            SSPMV_TRY(dalloc(&drows, rows.size(), s));
+            SSPMV_TRY(dalloc(&db, begin.size(), s));
+            SSPMV_TRY(dalloc(&dptr, optr.size(), s));
+            SSPMV_TRY(dalloc(&part, pieces.size() * kMaxK * sv, s));
+            SSPMV_TRY(dalloc(&opart, (size_t)nov * kMaxK * sv, s));
+            SSPMV_TRY(dalloc(&ocol, (size_t)novf, s));
+            SSPMV_TRY(dalloc(&oval, (size_t)novf * sv, s));
+            SSPMV_TRY(dalloc(&dov, (size_t)v.m, s));
+            SSPMV_CUDA_TRY(cudaMemcpyAsync(dp, pieces.data(), pieces.size() * sizeof(int4), cudaMemcpyHostToDevice, cu(s)));
+            SSPMV_CUDA_TRY(cudaMemcpyAsync(drows, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice, cu(s)));
+            SSPMV_CUDA_TRY(cudaMemcpyAsync(db, begin.data(), begin.size() * 4, cudaMemcpyHostToDevice, cu(s)));
+            SSPMV_CUDA_TRY(cudaMemcpyAsync(dptr, optr.data(), optr.size() * 8, cudaMemcpyHostToDevice, cu(s)));
+            SSPMV_CUDA_TRY(cudaMemsetAsync(dov, 0xff, (size_t)v.m * 4, cu(s)));
+            set_overflow_ids<<<grid_for(nov, 256), 256, 0, cu(s)>>>(nov, drows, dov);
+            SSPMV_LAUNCH_CHECK();
+            SSPMV_TRY(dispatch_value(f->value_type, [&](auto tag) -> sspmv_status {
+                using V = decltype(tag);
+                copy_overflow<V><<<grid_for(nov * 32, 256), 256, 0, cu(s)>>>(nov, v.C, drows, dptr, v.chunk_ptr, v.col,
+                                                                             (const V *)v.val, ocol, (V *)oval);
+                SSPMV_LAUNCH_CHECK();
+                return SSPMV_OK;
+            }));
+            SSPMV_CUDA_TRY(cudaStreamSynchronize(cu(s)));
+            dfree(dptr, s);
+            p->extra[0] = dp;
+            p->extra[1] = drows;
+            p->extra[2] = db;
+            p->extra[3] = part;
+            p->extra[4] = opart;
+            p->extra[5] = ocol;
+            p->extra[6] = oval;
+            p->extra[8] = dov;
+            p->extra_i[0] = (int64_t)pieces.size();
+            p->extra_i[1] = nov;
+        }
     }
     p->extra_i[7] = 1;
     return SSPMV_OK;
 }
 
-// kernel_flag 2 with C in {4, 8, 16} and k <= 2: chunk-group kernel;
-// otherwise a thread per row.
 template <typename V, int K>
-sspmv_status launch_sliced(const SlicedView &v, Plan *p, int kernel_flag, V alpha, const V *x, int64_t ldx, V beta,
-                           V *y, int64_t ldy, sspmv_stream_t s) {
-    const int64_t npieces = p ? p->extra_i[0] : 0;
-    const int64_t long_width = npieces > 0 ? kLongWidth : INT64_MAX;
-    bool grouped = false;
-    if constexpr (K <= 2) {
-        if (kernel_flag == 2 && v.nchunks > 0 && (v.C == 4 || v.C == 8 || v.C == 16)) {
-            grouped = true;
-            const int64_t warps = (v.nchunks + (32 / v.C) - 1) / (32 / v.C);
-            const unsigned grid = grid_for(warps * 32, kBlock, (int64_t)num_sms() * 16);
-            auto go = [&](auto kern) {
-                kern<<<grid, kBlock, 0, cu(s)>>>((int)v.m, v.nchunks, v.chunk_ptr, v.reorder, v.col,
-                                                (const V *)v.val, x, ldx, alpha, beta, y, ldy, long_width);
-            };
-            if (v.C == 4) go(sliced_group_kernel<V, K, 4>);
-            else if (v.C == 8) go(sliced_group_kernel<V, K, 8>);
-            else go(sliced_group_kernel<V, K, 16>);
-        }
-    }
-    if (!grouped) {
-        const unsigned grid = grid_for(v.m, kBlock, (int64_t)num_sms() * 16);
-        sliced_spmv_kernel<V, K><<<grid, kBlock, 0, cu(s)>>>((int)v.m, v.C, v.chunk_ptr, v.reorder, v.col,
-                                                             (const V *)v.val, x, ldx, alpha, beta, y, ldy,
-                                                             long_width);
-    }
+sspmv_status launch_sliced(const SlicedView &v, Plan *p, V alpha, const V *x, int64_t ldx, V beta, V *y,
+                           int64_t ldy, sspmv_stream_t s) {
+    const int64_t nov = p ? p->extra_i[1] : 0;
+    const unsigned grid = grid_for(v.m, kBlock, (int64_t)num_sms() * 16);
+    sliced_spmv_kernel<V, K><<<grid, kBlock, 0, cu(s)>>>(
+        (int)v.m, v.C, v.chunk_ptr, v.reorder, v.col, (const V *)v.val, x, ldx, alpha, beta, y, ldy,
+        nov > 0 ? kLongWidth : INT64_MAX, nov > 0 ? (const int32_t *)p->extra[8] : nullptr,
+        nov > 0 ? (V *)p->extra[4] : nullptr);
     SSPMV_LAUNCH_CHECK();
-    if (npieces > 0) {
-        const int64_t nlong = p->extra_i[1];
+    if (nov > 0) {
+        const int64_t npieces = p->extra_i[0];
         sliced_piece_kernel<V, K><<<grid_for(npieces * 32, kBlock), kBlock, 0, cu(s)>>>(
-            npieces, v.C, (const int4 *)p->extra[0], v.chunk_ptr, v.col, (const V *)v.val, x, ldx, (V *)p->extra[3]);
+            npieces, (const int4 *)p->extra[0], (const int32_t *)p->extra[5], (const V *)p->extra[6], x, ldx,
+            (V *)p->extra[3]);
         SSPMV_LAUNCH_CHECK();
-        sliced_piece_fixup<V, K><<<grid_for(nlong * v.C, 256), 256, 0, cu(s)>>>(
-            nlong, v.m, v.C, (const int32_t *)p->extra[1], (const int32_t *)p->extra[2], v.reorder,
+        sliced_piece_fixup<V, K><<<grid_for(nov, 256), 256, 0, cu(s)>>>(
+            nov, (const int32_t *)p->extra[1], (const int32_t *)p->extra[2], v.reorder, (const V *)p->extra[4],
             (const V *)p->extra[3], alpha, beta, y, ldy);
         SSPMV_LAUNCH_CHECK();
     }
@@ -393,10 +361,10 @@ sspmv_status spmm_sliced(const sspmv_features *f, const SlicedView &v, double al
         return for_rhs_chunks<V>(k, (const V *)X, (V *)Y, [&](int32_t step, const V *xs, V *ys) {
             const V a = (V)alpha, b = (V)beta;
             switch (step) {
-            case 8: return launch_sliced<V, 8>(v, p, f->kernel_flag, a, xs, ldx, b, ys, ldy, s);
-            case 4: return launch_sliced<V, 4>(v, p, f->kernel_flag, a, xs, ldx, b, ys, ldy, s);
-            case 2: return launch_sliced<V, 2>(v, p, f->kernel_flag, a, xs, ldx, b, ys, ldy, s);
-            default: return launch_sliced<V, 1>(v, p, f->kernel_flag, a, xs, ldx, b, ys, ldy, s);
+            case 8: return launch_sliced<V, 8>(v, p, a, xs, ldx, b, ys, ldy, s);
+            case 4: return launch_sliced<V, 4>(v, p, a, xs, ldx, b, ys, ldy, s);
+            case 2: return launch_sliced<V, 2>(v, p, a, xs, ldx, b, ys, ldy, s);
+            default: return launch_sliced<V, 1>(v, p, a, xs, ldx, b, ys, ldy, s);
             }
         });
     });

@@ -439,11 +439,11 @@ __device__ __forceinline__ void stream_load8(const int32_t *__restrict__ ci, con
     }
 }
 
-// The stream kernel for FP64 with k >= 4 right-hand sides: groups of G = k
+// The stream kernel for FP64 with k = 8 right-hand sides: groups of G = k
 // lanes share a run of 8G consecutive nonzeros, lane q of a group owning column q,
 // so each gathered row X[col, 0:k] (k consecutive values) is read by G
 // adjacent lanes in one coalesced access instead of k scattered loads by one
-// lane.  A group walks its nonzeros in order (loads of 16 in flight) with the
+// lane.  A group walks its nonzeros in order (loads of 8 in flight) with the
 // row logic of the per-lane form; the groups' open sums are joined by a
 // segmented shuffle scan with stride G.
 template <typename V, int K, int G>
@@ -488,7 +488,7 @@ __device__ __forceinline__ void stream_chunk_cols(
     for (int q = 0; q < KL; q++) seg[q] = head[q] = V(0);
     bool any_end = false, last_open = false;
     int head_row = -1, last_row = -1;
-    constexpr int SB = 16;  // nonzeros whose loads are in flight together
+    constexpr int SB = 8;  // nonzeros whose loads are in flight together
     for (int s0 = 0; s0 < nv; s0 += SB) {  // group-uniform
         int c[SB];
         V a[SB], xv[SB][KL];
@@ -720,16 +720,17 @@ __device__ __forceinline__ void stream_chunk_lanes(
     }
 }
 
-// One lane per nonzero run (stream_chunk_lanes), except FP64 with k = 4, 8:
-// column groups (stream_chunk_cols), which read each 32- or 64-byte row of X
-// with one coalesced access (measured faster there, slower for FP32).
+// One lane per nonzero run (stream_chunk_lanes), except FP64 with k = 8:
+// column groups (stream_chunk_cols), which read each 64-byte row of X with
+// one coalesced access (measured 1.3-1.4x faster there; slower for FP32 and
+// mixed for k = 4).
 template <typename V, int K>
 __device__ __forceinline__ void stream_chunk(
     int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
     const int32_t *__restrict__ row_start, const int64_t w, const int64_t slot, int32_t *__restrict__ carry_row,
     int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val, int vec) {
-    if constexpr (K >= 4 && sizeof(V) == 8)
+    if constexpr (K == 8 && sizeof(V) == 8)
         stream_chunk_cols<V, K, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, slot, carry_row,
                                    has_end, carry_val, head_val);
     else

@@ -115,15 +115,10 @@ ORACLE_CONV = {
     "csr5": lambda O, A: O.csr_to_csr5(A),
     "csr5_w32": lambda O, A: O.csr_to_csr5(A, 16, 32),
     "csr5_s12_w4": lambda O, A: O.csr_to_csr5(A, 12, 4),
-    "sell_c4_warp": lambda O, A: O.csr_to_sell(A, 4, 4),
-    "scs_c8_warp": lambda O, A: O.csr_to_sell_c_sigma(A, 256, 8, 1),
-    "scr_c16_warp": lambda O, A: O.csr_to_sell_c_R(A, 16),
+    "sell_c4": lambda O, A: O.csr_to_sell(A, 4, 4),
+    "scs_c8": lambda O, A: O.csr_to_sell_c_sigma(A, 256, 8, 1),
+    "scr_c16": lambda O, A: O.csr_to_sell_c_R(A, 16),
 }
-
-
-def _kernel(M, flag):
-    M.set_kernel(flag, 0)
-    return M
 
 
 GPU_CONV = {
@@ -139,10 +134,10 @@ GPU_CONV = {
     "csr5": lambda L, M: L.csr_to_csr5(M),
     "csr5_w32": lambda L, M: L.csr_to_csr5(M, 16, 32),
     "csr5_s12_w4": lambda L, M: L.csr_to_csr5(M, 12, 4),
-    # the warp-per-chunk-group sliced kernel (kernel_flag 2)
-    "sell_c4_warp": lambda L, M: _kernel(L.csr_to_sell(M, 4, 4), 2),
-    "scs_c8_warp": lambda L, M: _kernel(L.csr_to_sell_c_sigma(M, 256, 8, 1), 2),
-    "scr_c16_warp": lambda L, M: _kernel(L.csr_to_sell_c_R(M, 16), 2),
+    # narrow chunks: long rows in the compact overflow path
+    "sell_c4": lambda L, M: L.csr_to_sell(M, 4, 4),
+    "scs_c8": lambda L, M: L.csr_to_sell_c_sigma(M, 256, 8, 1),
+    "scr_c16": lambda L, M: L.csr_to_sell_c_R(M, 16),
 }
 
 
