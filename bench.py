@@ -12,7 +12,9 @@ A step is one SpMV (y = A*x, alpha=1, beta=0) of every feasible
 value = sum of algorithmic bytes / sum of kernel time (GB/s), device-resident
 inputs, L2 flushed (256 MiB write) before every SpMV and excluded from the
 timing.  e2e = the same through the C ABI with pinned host x copied in and y
-copied out inside the timed region of every SpMV.
+copied out of every SpMV inside the timed region, the copies on their own
+streams overlapping the other matrices' SpMVs (serial_value: copies and SpMV
+back to back on one stream).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl sspmv|reference]
 """
@@ -37,6 +39,7 @@ sys.path.insert(0, str(ROOT))
 FAMILIES = ["banded_2M", "powerlaw_4M", "block4_2M", "uniform_4M"]
 DTYPES = ["f64", "f32"]
 L2_FLUSH_BYTES = 256 << 20
+RANDOM_COLUMN_FAMILIES = ("uniform_4M", "powerlaw_4M")
 
 
 def parse_args():
@@ -250,6 +253,9 @@ def run_gpu(args, rank, world):
     _barrier(world)
     log("timed steps done")
 
+    parity = check_cases(cases, hosts)
+    log("parity checked")
+
     per_case = []
     total_ms = 0.0
     total_bytes = 0.0
@@ -261,7 +267,7 @@ def run_gpu(args, rank, world):
         per_case.append({"family": c["fam"], "format": c["fmt"], "dtype": c["dt"], "ms": round(avg, 5),
                          "GBps": round(c["bytes"] / avg / 1e6, 1),
                          "GFLOPs": round(2.0 * c["nnz"] / avg / 1e6, 1),
-                         "kernel": c["tuned"] or c["kernel"]})
+                         "kernel": c["tuned"] or c["kernel"], "max_norm_err": c["max_norm_err"]})
     step_ms = total_ms / args.steps
     step_ms = _max_over_ranks(step_ms, world)
     value = total_bytes / args.steps * world / (step_ms * 1e6)
@@ -281,6 +287,27 @@ def run_gpu(args, rank, world):
                 "traffic": tt["bytes_per_launch"] if tt else None,
                 "kernel": f"{dc['fam']}/{dc['fmt']}/{dc['dt']}",
                 "algorithmic_bytes": dc["bytes"]}
+    if rank == 0:
+        # random column indices: the x gathers, not HBM, bound the kernels; the
+        # gather ceiling is measured live for each such matrix's x size and
+        # gather count (one gather per nonzero)
+        from sspmv_gb300 import lespmv as L
+        ceiling = {}
+        for c, pc in zip(cases, per_case):
+            if c["fam"] not in RANDOM_COLUMN_FAMILIES:
+                continue
+            key = (c["fam"], c["dt"])
+            if key not in ceiling:
+                ceiling[key] = L.gather_ceiling(np_dtype(c["dt"]), c["cols"], min(c["nnz"], 1 << 28))[0]
+            pc["gather_frac"] = round(c["nnz"] / (pc["ms"] * 1e-3) / ceiling[key], 4)
+        key = (dc["fam"], dc["dt"])
+        rate = ceiling.get(key) or L.gather_ceiling(np_dtype(dc["dt"]), dc["cols"], min(dc["nnz"], 1 << 28))[0]
+        kernel_rate = dc["nnz"] / (per_case[dom]["ms"] * 1e-3)
+        roofline["gather_ceiling"] = {
+            "ceiling_gathers_per_s": round(rate, 1), "achieved_gathers_per_s": round(kernel_rate, 1),
+            "frac": round(kernel_rate / rate, 4),
+            "what": "one x gather per nonzero; ceiling = random gathers from a vector of the same size, "
+                    "indices streamed (sspmv_gather_ceiling)"}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(hosts, families, dtypes, fmts, budget_s=15.0)
@@ -310,6 +337,7 @@ def run_gpu(args, rank, world):
                    "alpha": 1.0, "beta": 0.0, "k_rhs": 1, "index": "int32", "parallelism": f"replicas{world}",
                    "skipped": skipped, "scale": args.scale},
         "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches),
+        "parity": parity,
         "wall_s": round(wall, 3), "per_format": per_case, "laplacian_1024": lap, "large_powerlaw_16M": large,
         "serving": serving,
     }
@@ -321,16 +349,43 @@ def _x_host(n, dt):
 
 
 def run_e2e(args, cases, flush, stream, world):
-    """Same sweep through the public call with host buffers: pinned x copied
-    in, SpMV, y copied out, all inside the CUDA-event bracket of each SpMV."""
+    """The same sweep through the public call with host buffers: pinned x
+    copied in, SpMV, y copied out, every step.
+
+    value: the copies run on their own streams (host-to-device, device-to-
+    host) and overlap the SpMVs of other matrices: x of matrix i+1 moves while
+    matrix i multiplies, y of matrix i while matrix i+1 multiplies.  One event
+    bracket per sweep; the sweep's matrices total far more than L2, so there
+    is no flush inside it.  serial_value: each SpMV with its own copies in one
+    bracket on one stream (L2 flushed before each, flush not timed)."""
     import torch
     from sspmv_gb300 import lespmv as L
     hx = [c["x"].cpu().pin_memory() for c in cases]
     hy = [torch.empty(c["rows"], dtype=c["y"].dtype).pin_memory() for c in cases]
     h2d = sum(t.numel() * t.element_size() for t in hx)
     d2h = sum(t.numel() * t.element_size() for t in hy)
-    total_ms, total_bytes = 0.0, 0.0
-    for step in range(args.warmup + args.steps):
+    step_bytes = float(sum(c["bytes"] for c in cases))
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def overlapped():
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        s_in.wait_stream(stream)
+        s_out.wait_stream(stream)
+        for i, c in enumerate(cases):
+            with torch.cuda.stream(s_in):
+                c["x"].copy_(hx[i], non_blocking=True)
+            stream.wait_stream(s_in)
+            L.LeSpMV(1.0, c["M"], c["x"], 0.0, c["y"], stream)
+            s_out.wait_stream(stream)
+            with torch.cuda.stream(s_out):
+                hy[i].copy_(c["y"], non_blocking=True)
+        stream.wait_stream(s_out)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        return t0.elapsed_time(t1)
+
+    def serial():
         pairs = []
         for i, c in enumerate(cases):
             flush.zero_()
@@ -340,15 +395,55 @@ def run_e2e(args, cases, flush, stream, world):
             L.LeSpMV(1.0, c["M"], c["x"], 0.0, c["y"], stream)
             hy[i].copy_(c["y"], non_blocking=True)
             e1.record(stream)
-            pairs.append((e0, e1, c["bytes"]))
+            pairs.append((e0, e1))
         torch.cuda.synchronize()
-        if step >= args.warmup:
-            for e0, e1, b in pairs:
-                total_ms += e0.elapsed_time(e1)
-                total_bytes += b
-    step_ms = _max_over_ranks(total_ms / args.steps, world)
-    return {"value": round(total_bytes / args.steps * world / (step_ms * 1e6), 1), "unit": "GB/s",
-            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": round(step_ms, 4)}
+        return sum(a.elapsed_time(b) for a, b in pairs)
+
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            overlapped()
+        ov = sum(overlapped() for _ in range(args.steps)) / args.steps
+        for _ in range(args.warmup):
+            serial()
+        se = sum(serial() for _ in range(args.steps)) / args.steps
+    ov = _max_over_ranks(ov, world)
+    se = _max_over_ranks(se, world)
+    return {"value": round(step_bytes * world / (ov * 1e6), 1), "unit": "GB/s",
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": round(ov, 4),
+            "copies": "pinned host x in and y out of every SpMV on two copy streams, overlapping other SpMVs",
+            "serial_value": round(step_bytes * world / (se * 1e6), 1), "serial_ms_per_step": round(se, 4)}
+
+
+# ------------------------------------------------------- result checking --
+def check_cases(cases, hosts):
+    """Every timed matrix's last y (= A x) on sampled rows -- every 61st row
+    and the 64 longest -- against an FP64 product on the same inputs, in units
+    of the per-row bound 8 nnz_i eps sum_j |a_ij x_j| (eps of the value type)."""
+    import scipy.sparse as sp
+    refs = {}
+    worst = 0.0
+    for c in cases:
+        key = (c["fam"], c["dt"])
+        if key not in refs:
+            A = hosts[key]
+            lens = np.diff(A.row_offset)
+            rows = np.union1d(np.arange(0, A.num_rows, 61), np.argsort(lens)[-64:])
+            sub_ptr = np.concatenate([[0], np.cumsum(lens[rows])])
+            take = np.repeat(A.row_offset[rows] - sub_ptr[:-1], lens[rows]) + np.arange(sub_ptr[-1])
+            Asp = sp.csr_matrix((A.values[take].astype(np.float64), A.col_index[take], sub_ptr),
+                                shape=(len(rows), A.num_cols))
+            x64 = _x_host(A.num_cols, c["dt"]).astype(np.float64)
+            eps = np.finfo(A.values.dtype).eps
+            bound = 8.0 * np.maximum(lens[rows], 1) * eps * (abs(Asp) @ np.abs(x64)) + np.finfo(np.float64).tiny
+            refs[key] = (rows, Asp @ x64, bound)
+        rows, y64, bound = refs[key]
+        yg = c["y"].cpu().numpy()[rows].astype(np.float64)
+        c["max_norm_err"] = round(float((np.abs(yg - y64) / bound).max(initial=0.0)), 4)
+        worst = max(worst, c["max_norm_err"])
+    return {"cases": len(cases), "rows": "every 61st and the 64 longest of each matrix",
+            "max_norm_err": worst, "within_tolerance": bool(worst <= 1.0),
+            "tolerance": "|y - y_fp64| <= 8 nnz_i eps sum_j |a_ij x_j| per row"}
 
 
 # ------------------------------------------------ large power-law section --

@@ -208,9 +208,21 @@ const char *sspmv_last_error(void);
 const char *sspmv_version(void);
 /* Number of kernels this library has launched in the process so far. */
 int64_t sspmv_launch_count(void);
+/* Measured ceiling of random gathers from a vector of num_cols values of
+ * value_type: num_gathers (rounded down to a multiple of 256) uniformly
+ * spread indices streamed once, 8 read-only gathers in flight per lane, the
+ * pattern of SpMV on matrices with random column indices.  Best of 5 timed
+ * launches after 3 warm-up ones, in gathers per second; checksum (optional)
+ * is the sum of the per-thread sums.  A measurement utility of this library
+ * (no reference counterpart); allocates and frees its own buffers. */
+sspmv_status sspmv_gather_ceiling(int32_t value_type, int64_t num_cols, int64_t num_gathers,
+                                  double *gathers_per_second, double *checksum, sspmv_stream_t stream);
 /* Selects the SpMV kernel of a matrix (pass &A->f): kernel_flag as in each
- * format's LeSpMV entry, param a kernel parameter (CSR vector kernel: lanes
- * per row 2..32; 0 lets the library choose).  Used by the autotuner. */
+ * format's LeSpMV entry, param a kernel parameter (0 lets the library
+ * choose): CSR vector kernel: lanes per row 2..32; S-ELL, SELL-c-sigma,
+ * SELL-c-R: the slots a row's thread reads before the rest of the row moves
+ * to the overflow CSR pass (default: a cost model over the row lengths).
+ * Used by the autotuner. */
 sspmv_status sspmv_set_kernel(sspmv_features *f, int32_t kernel_flag, int32_t param);
 
 /* ---------------- CSR creation ---------------- */

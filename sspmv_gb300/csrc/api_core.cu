@@ -36,14 +36,14 @@ sspmv_status fail(sspmv_status s, const char *fmt, ...) {
     return s;
 }
 
-std::mutex &plan_mutex() {
-    static std::mutex m;
+PlanMutex &plan_mutex() {
+    static PlanMutex m;
     return m;
 }
 
 Plan *get_plan(const sspmv_features *f) {
     if (f->priv) return reinterpret_cast<Plan *>(f->priv);
-    std::lock_guard<std::mutex> g(plan_mutex());
+    std::lock_guard<PlanMutex> g(plan_mutex());
     if (!f->priv) const_cast<sspmv_features *>(f)->priv = new (std::nothrow) Plan();
     return reinterpret_cast<Plan *>(f->priv);
 }
@@ -57,6 +57,10 @@ void free_plan(sspmv_features *f, sspmv_stream_t s) {
         dfree(mp.has_end, s);
         dfree(mp.carry_val, s);
         dfree(mp.head_val, s);
+    }
+    if (p->sub) {
+        free_plan(&p->sub->f, s);
+        delete p->sub;
     }
     for (void *e : p->extra) dfree(e, s);
     delete p;

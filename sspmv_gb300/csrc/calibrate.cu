@@ -1,0 +1,127 @@
+// calibrate.cu -- the measured ceiling of random gathers from the x vector.
+//
+// SpMV on matrices whose column indices are spread at random (uniform,
+// power-law) is bound by the x gathers, not by HBM: every gathered element
+// costs one L1 line lookup (a warp's gather touches 32 distinct lines) and
+// one 32-byte L2 sector, while x itself (tens of MB) stays in L2.  This kernel
+// runs that access pattern alone -- indices streamed once with evict-first
+// loads, 8 read-only gathers in flight per lane, one sum per thread -- so
+// a kernel's gather rate can be set against what the GPU delivers for the
+// same pattern.
+#include "common.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace sspmv {
+namespace {
+
+constexpr int kPerLane = 8;
+constexpr int kBlockG = 256;
+
+// Index i of the gather sequence: a 64-bit mix (splitmix64 finaliser) of i,
+// reduced to [0, n).
+__global__ void gather_indices(int64_t count, int64_t n, uint64_t seed, int32_t *__restrict__ idx) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t z = (uint64_t)i + seed + 0x9E3779B97F4A7C15ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        idx[i] = (int32_t)(z % (uint64_t)n);
+    }
+}
+
+template <typename V>
+__global__ void fill_x(int64_t n, V *__restrict__ x) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = V(1) + V(i % 7) * V(0.125);
+}
+
+// Warp w takes runs of 256 indices w, w + warps, ...; lane l its 8
+// consecutive indices of each run.
+template <typename V>
+__global__ void __launch_bounds__(kBlockG) gather_kernel(const V *__restrict__ x, const int32_t *__restrict__ idx,
+                                                         int64_t runs, V *__restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    V acc = V(0);
+    for (int64_t w = w0; w < runs; w += nw) {
+        const int4 *ip = reinterpret_cast<const int4 *>(idx + w * 32 * kPerLane + lane * kPerLane);
+        const int4 a = ld_stream(ip), b = ld_stream(ip + 1);
+        const int c[kPerLane] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        V v[kPerLane];
+#pragma unroll
+        for (int u = 0; u < kPerLane; u++) v[u] = ld_x(x + c[u]);
+#pragma unroll
+        for (int u = 0; u < kPerLane; u++) acc += v[u];
+    }
+    out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+
+}  // namespace
+}  // namespace sspmv
+
+using namespace sspmv;
+
+extern "C" sspmv_status sspmv_gather_ceiling(int32_t value_type, int64_t num_cols, int64_t num_gathers,
+                                             double *gathers_per_second, double *checksum, sspmv_stream_t stream) {
+    if (!valid_vt(value_type)) return fail(SSPMV_INVALID_ARG, "unknown value_type %d", value_type);
+    if (!gathers_per_second || num_cols <= 0 || num_cols > 0x7fffffff || num_gathers <= 0)
+        return fail(SSPMV_INVALID_ARG, "gather ceiling: num_cols in [1, 2^31) and num_gathers > 0 required");
+    const int64_t per_run = 32 * kPerLane;
+    const int64_t runs = std::max<int64_t>(num_gathers / per_run, 1);
+    const int64_t count = runs * per_run;
+    const unsigned grid = (unsigned)(num_sms() * 8);  // 8 resident 256-thread CTAs per SM
+    int32_t *idx = nullptr;
+    void *x = nullptr, *out = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    const size_t sv = vsize(value_type);
+    sspmv_status st = SSPMV_OK;
+    float best = 0.f;
+    auto body = [&]() -> sspmv_status {
+        SSPMV_TRY(dalloc(&idx, (size_t)count, stream));
+        SSPMV_TRY(dalloc((unsigned char **)&x, (size_t)num_cols * sv, stream));
+        SSPMV_TRY(dalloc((unsigned char **)&out, (size_t)grid * kBlockG * sv, stream));
+        gather_indices<<<grid_for(count, 256, (int64_t)num_sms() * 32), 256, 0, cu(stream)>>>(count, num_cols, 12345,
+                                                                                              idx);
+        SSPMV_LAUNCH_CHECK();
+        SSPMV_CUDA_TRY(cudaEventCreate(&e0));
+        SSPMV_CUDA_TRY(cudaEventCreate(&e1));
+        return dispatch_value(value_type, [&](auto tag) -> sspmv_status {
+            using V = decltype(tag);
+            fill_x<V><<<grid_for(num_cols, 256, (int64_t)num_sms() * 32), 256, 0, cu(stream)>>>(num_cols, (V *)x);
+            SSPMV_LAUNCH_CHECK();
+            for (int rep = 0; rep < 8; rep++) {  // 3 warm-up launches, best of 5 timed
+                SSPMV_CUDA_TRY(cudaEventRecord(e0, cu(stream)));
+                gather_kernel<V><<<grid, kBlockG, 0, cu(stream)>>>((const V *)x, idx, runs, (V *)out);
+                SSPMV_LAUNCH_CHECK();
+                SSPMV_CUDA_TRY(cudaEventRecord(e1, cu(stream)));
+                SSPMV_CUDA_TRY(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                SSPMV_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+                if (rep >= 3 && (best == 0.f || ms < best)) best = ms;
+            }
+            if (checksum) {
+                std::vector<V> h((size_t)grid * kBlockG);
+                SSPMV_CUDA_TRY(cudaMemcpyAsync(h.data(), out, h.size() * sizeof(V), cudaMemcpyDeviceToHost,
+                                               cu(stream)));
+                SSPMV_CUDA_TRY(cudaStreamSynchronize(cu(stream)));
+                double s = 0;
+                for (V v : h) s += (double)v;
+                *checksum = s;
+            }
+            return SSPMV_OK;
+        });
+    };
+    st = body();
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    dfree(idx, stream);
+    dfree(x, stream);
+    dfree(out, stream);
+    if (st != SSPMV_OK) return st;
+    cudaStreamSynchronize(cu(stream));
+    *gathers_per_second = (double)count / ((double)best * 1e-3);
+    return SSPMV_OK;
+}

@@ -443,30 +443,23 @@ __global__ void coo_fixup(int64_t ntiles, const int32_t *__restrict__ ri, int ti
                           const int32_t *__restrict__ carry_row, const int32_t *__restrict__ has_end,
                           const V *__restrict__ carry_val, const V *__restrict__ head_val, V alpha, V beta,
                           V *__restrict__ y, int64_t ldy) {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntiles) return;
-    const int r = carry_row[t];
-    if (r < 0) return;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t - (threadIdx.x & 31) >= ntiles) return;  // whole warp past the end
+    const int r = t < ntiles ? carry_row[t] : -1;
     // owner: the tile where row r starts (it does not continue from tile t-1,
     // or tile t holds other rows before it)
-    const int64_t j0 = t * (int64_t)tile;
-    const bool starts_here = !(ri[j0] == r && j0 > 0 && ri[j0 - 1] == r);
-    if (!starts_here) return;
-    V tot[K];
-#pragma unroll
-    for (int q = 0; q < K; q++) tot[q] = carry_val[t * kMaxK + q];
-    for (int64_t u = t + 1; u < ntiles; u++) {
-        if (has_end[u]) {
-#pragma unroll
-            for (int q = 0; q < K; q++) tot[q] += head_val[u * kMaxK + q];
-            break;
-        }
-#pragma unroll
-        for (int q = 0; q < K; q++) tot[q] += carry_val[u * kMaxK + q];
+    bool mine = false;
+    if (r >= 0) {
+        const int64_t j0 = t * (int64_t)tile;
+        mine = !(ri[j0] == r && j0 > 0 && ri[j0 - 1] == r);
     }
-    V *yp = y + (int64_t)r * ldy;
+    V tot[K];
+    chain_sum<V, K>(mine, t, ntiles, 0, has_end, carry_val, head_val, tot);
+    if (mine) {
+        V *yp = y + (int64_t)r * ldy;
 #pragma unroll
-    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
+        for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
+    }
 }
 
 struct CooPlan {
@@ -480,7 +473,7 @@ struct CooPlan {
 // extra[0..]: carry buffers per tile size, extra[10] = absent-row list (extra[6..8]: warp chunks)
 sspmv_status ensure_coo_plan(const sspmv_coo *A, Plan *p, int which, int tile, sspmv_stream_t s) {
     if (p->extra[which * 3]) return SSPMV_OK;
-    std::lock_guard<std::mutex> g(plan_mutex());
+    std::lock_guard<PlanMutex> g(plan_mutex());
     if (p->extra[which * 3]) return SSPMV_OK;
     const int64_t nnz = A->f.num_nnzs, m = A->f.num_rows;
     const int64_t nt = std::max<int64_t>((nnz + tile - 1) / tile, 1);

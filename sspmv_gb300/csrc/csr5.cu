@@ -223,7 +223,9 @@ __device__ __forceinline__ uint32_t c5_bit(const uint32_t *d, int lane, int i, i
     return (w >> (31 - glid % 32)) & 1u;
 }
 
-template <typename V, int K, int OMEGA>
+// SIG > 0: sigma known at compile time (16 or 32, descriptors of at most two
+// packets), so a lane's loop over its sigma nonzeros unrolls fully.
+template <typename V, int K, int OMEGA, int SIG>
 __global__ void __launch_bounds__(kBlock) csr5_tile_kernel(C5View A, const V *__restrict__ x, int64_t ldx, V alpha,
                                                          V beta, V *__restrict__ y, int64_t ldy,
                                                          int32_t *__restrict__ carry_row, int32_t *__restrict__ has_end,
@@ -235,7 +237,7 @@ __global__ void __launch_bounds__(kBlock) csr5_tile_kernel(C5View A, const V *__
     const int64_t t = warp * kGroups + g;
     const bool active = t < (int64_t)A.p - 1;
     const V *val = (const V *)A.val;
-    const int sigma = A.sigma;
+    const int sigma = SIG > 0 ? SIG : A.sigma;
     const int64_t tile = (int64_t)sigma * OMEGA;
     const int64_t base = t * tile;
 
@@ -265,11 +267,26 @@ __global__ void __launch_bounds__(kBlock) csr5_tile_kernel(C5View A, const V *__
     for (int q = 0; q < K; q++) sum[q] = head[q] = V(0);
     bool seen = false;
     int32_t rel = yoff;
-    const uint32_t bit0 = active ? c5_bit<OMEGA>(dl, xl, 0, A.bao, d0) : 0u;
+    // With at most two descriptor packets the lane's flags for positions
+    // 0..sigma-1 fit one 64-bit window: position i at bit 63 - i.
+    const bool window = SIG > 0 || A.np <= 2;
+    uint64_t bits = 0;
+    if (active && window)
+        bits = ((uint64_t)d0 << 32 | (A.np > 1 ? dl[OMEGA + xl] : 0u)) << A.bao;
+    auto bit_at = [&](int i) -> uint32_t {
+        if (window) return (uint32_t)(bits >> (63 - i)) & 1u;
+        return c5_bit<OMEGA>(dl, xl, i, A.bao, d0);
+    };
+    const uint32_t bit0 = active ? bit_at(0) : 0u;
     if (active) {
+        // lane xl's i-th nonzero: p0 + i * step (tiles inside one row are
+        // stored untransposed)
+        const int64_t p0 = fast ? base + (int64_t)xl * sigma : base + xl;
+        const int64_t step = fast ? 1 : OMEGA;
         // nonzeros whose loads (and x gathers) are in flight together: 8 for
         // f32 at k = 1; 4 otherwise (deeper prefetch measured slower for f64)
         constexpr int kU = (sizeof(V) == 4 && K == 1) ? 8 : 4;
+#pragma unroll
         for (int i0 = 0; i0 < sigma; i0 += kU) {
             int cc[kU];
             V aa[kU], xv[kU][K];
@@ -279,7 +296,7 @@ __global__ void __launch_bounds__(kBlock) csr5_tile_kernel(C5View A, const V *__
                 cc[u] = 0;
                 aa[u] = V(0);
                 if (i < sigma) {
-                    const int64_t idx = fast ? base + (int64_t)xl * sigma + i : base + (int64_t)i * OMEGA + xl;
+                    const int64_t idx = p0 + (int64_t)i * step;
                     cc[u] = ld_stream(A.col + idx);
                     aa[u] = ld_stream(val + idx);
                 }
@@ -292,7 +309,7 @@ __global__ void __launch_bounds__(kBlock) csr5_tile_kernel(C5View A, const V *__
             for (int u = 0; u < kU; u++) {
                 const int i = i0 + u;
                 if (i >= sigma) break;
-                const uint32_t b = (xl == 0 && i == 0) ? 0u : (i == 0 ? bit0 : c5_bit<OMEGA>(dl, xl, i, A.bao, d0));
+                const uint32_t b = (xl == 0 && i == 0) ? 0u : (i == 0 ? bit0 : bit_at(i));
                 if (b) {
                     if (!seen) {
 #pragma unroll
@@ -437,25 +454,17 @@ __global__ void csr5_fixup(int32_t ntiles, int64_t tile, const int32_t *__restri
                            const int32_t *__restrict__ carry_row, const int32_t *__restrict__ has_end,
                            const V *__restrict__ carry_val, const V *__restrict__ head_val, V alpha, V beta,
                            V *__restrict__ y, int64_t ldy) {
-    int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntiles - 1) return;
-    const int32_t r = carry_row[t];
-    if (r < 0 || (int64_t)rp[r] < (int64_t)t * tile) return;  // row began in an earlier tile
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t - (threadIdx.x & 31) >= ntiles - 1) return;  // whole warp past the last full tile
+    const int32_t r = t < ntiles - 1 ? carry_row[t] : -1;
+    const bool mine = r >= 0 && (int64_t)rp[r] >= t * tile;  // open here and began in tile t
     V tot[K];
+    chain_sum<V, K>(mine, t, ntiles, 0, has_end, carry_val, head_val, tot);
+    if (mine) {
+        V *yp = y + (int64_t)r * ldy;
 #pragma unroll
-    for (int q = 0; q < K; q++) tot[q] = carry_val[(int64_t)t * kMaxK + q];
-    for (int32_t u = t + 1; u < ntiles; u++) {
-        if (has_end[u]) {
-#pragma unroll
-            for (int q = 0; q < K; q++) tot[q] += head_val[(int64_t)u * kMaxK + q];
-            break;
-        }
-#pragma unroll
-        for (int q = 0; q < K; q++) tot[q] += carry_val[(int64_t)u * kMaxK + q];
+        for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
     }
-    V *yp = y + (int64_t)r * ldy;
-#pragma unroll
-    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
 }
 
 C5View view_of(const sspmv_csr5 *A) {
@@ -480,7 +489,7 @@ C5View view_of(const sspmv_csr5 *A) {
 // plan: extra[0] carry_row+has_end ints (2p), extra[1] carry_val, extra[2] head_val
 sspmv_status ensure_c5_plan(const sspmv_csr5 *A, Plan *pl, sspmv_stream_t s) {
     if (pl->extra[0]) return SSPMV_OK;
-    std::lock_guard<std::mutex> g(plan_mutex());
+    std::lock_guard<PlanMutex> g(plan_mutex());
     if (pl->extra[0]) return SSPMV_OK;
     const int64_t p = std::max<int64_t>(A->_p, 1);
     const size_t sv = vsize(A->f.value_type);
@@ -515,8 +524,23 @@ sspmv_status launch_c5_tiles(const C5View &v, V alpha, const V *x, int64_t ldx, 
                              int32_t *cr, int32_t *he, V *cv, V *hv, sspmv_stream_t s) {
     const int64_t tiles = v.p - 1;
     const int64_t warps = (tiles + (32 / OMEGA) - 1) / (32 / OMEGA);
-    csr5_tile_kernel<V, K, OMEGA><<<grid_for(warps * 32, kBlock), kBlock, 0, cu(s)>>>(v, x, ldx, alpha, beta, y, ldy,
-                                                                                     cr, he, cv, hv);
+    const unsigned grid = grid_for(warps * 32, kBlock);
+    const int sig = (v.np <= 2 && (v.sigma == 16 || v.sigma == 32)) ? v.sigma : 0;
+    if constexpr (K == 1) {  // one right-hand side: sigma-specialised kernels
+        if (sig == 16) {
+            csr5_tile_kernel<V, K, OMEGA, 16><<<grid, kBlock, 0, cu(s)>>>(v, x, ldx, alpha, beta, y, ldy, cr, he, cv,
+                                                                          hv);
+            SSPMV_LAUNCH_CHECK();
+            return SSPMV_OK;
+        }
+        if (sig == 32) {
+            csr5_tile_kernel<V, K, OMEGA, 32><<<grid, kBlock, 0, cu(s)>>>(v, x, ldx, alpha, beta, y, ldy, cr, he, cv,
+                                                                          hv);
+            SSPMV_LAUNCH_CHECK();
+            return SSPMV_OK;
+        }
+    }
+    csr5_tile_kernel<V, K, OMEGA, 0><<<grid, kBlock, 0, cu(s)>>>(v, x, ldx, alpha, beta, y, ldy, cr, he, cv, hv);
     SSPMV_LAUNCH_CHECK();
     return SSPMV_OK;
 }

@@ -31,9 +31,14 @@ struct Plan {
     int param = 0;          // kernel parameter set by sspmv_set_kernel (0 = library choice)
     void *extra[12] = {nullptr};  // format-specific device buffers
     int64_t extra_i[12] = {0};
+    sspmv_csr *sub = nullptr;     // a library-made CSR view over extra buffers (its own plan freed with this one)
 };
 
-std::mutex &plan_mutex();
+// Guards plan creation.  Recursive: building one plan may build another
+// (a sliced matrix's overflow CSR gets its stream plan while its own plan is
+// being built).
+using PlanMutex = std::recursive_mutex;
+PlanMutex &plan_mutex();
 Plan *get_plan(const sspmv_features *f);  // creates an empty plan if needed
 void free_plan(sspmv_features *f, sspmv_stream_t s);
 

@@ -24,6 +24,7 @@
 #include "common.cuh"
 #include "plan.cuh"
 #include "primitives.cuh"
+#include "serve.cuh"
 #include "spmv_common.cuh"
 
 namespace sspmv {
@@ -39,29 +40,27 @@ constexpr int kBlock = 256;
 
 // ------------------------------------------------------------------ SpMV --
 // A thread per stored row reads its slots (C consecutive rows read together)
-// up to its first padding slot.  In chunks wider than kLongWidth slots only
-// the first kLongWidth are read this way (a 38k-slot row would serialise its
-// warp): the slots past them of each row that goes on (the "overflow", found
-// once per matrix) are copied into compact arrays when the plan is built,
-// summed there in pieces of about kPieceElems nonzeros, one warp each, and a
-// fix-up adds a row's thread partial and its pieces in order.  The compact
-// copy reads only the long rows' nonzeros, not the padding of the short rows
-// sharing their chunks (slot-major storage puts them in the same sectors).
-constexpr int64_t kLongWidth = 64;
-constexpr int64_t kPieceElems = 2048;
-
+// up to its first padding slot, so a warp runs as long as its longest row.
+// Where a few long rows would keep most lanes of their warps idle, the
+// thread pass stops at a cap (chosen once per matrix by choose_cap): the rest
+// of each longer row (its "overflow") is copied once into compact arrays.
+// Short tails form a CSR matrix multiplied by the CSR stream kernel (every
+// lane busy whatever the row lengths); long tails are cut into pieces of one
+// row, a warp each; a fix-up adds each overflow row's thread partial and the
+// rest.  The compact copy also skips the padding of the short rows that
+// share a long row's chunk (slot-major storage puts them in the same sectors).
 template <typename V, int K>
 __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
     int m, int C, const int64_t *__restrict__ chunk_ptr, const int32_t *__restrict__ reorder,
     const int32_t *__restrict__ col, const V *__restrict__ val, const V *__restrict__ x, int64_t ldx, V alpha,
-    V beta, V *__restrict__ y, int64_t ldy, int64_t long_width, const int32_t *__restrict__ ovf_id,
+    V beta, V *__restrict__ y, int64_t ldy, int64_t cap, const int32_t *__restrict__ ovf_id,
     V *__restrict__ ovf_part) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t c = i / C;
         const int r = (int)(i - c * C);
         const int64_t base = ld_stream(chunk_ptr + c);
         const int64_t wfull = (ld_stream(chunk_ptr + c + 1) - base) / C;
-        const int64_t w = min(wfull, long_width);
+        const int64_t w = min(wfull, cap);
         const int32_t *cp = col + base + r;
         const V *vp = val + base + r;
         V s[K];
@@ -93,7 +92,7 @@ __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
                 for (int q = 0; q < K; q++) s[q] += aa * ld_x(x + (int64_t)cc * ldx + q);
             }
         }
-        if (wfull > w && ld_stream(cp + w * C) >= 0) {  // the row goes on: overflow
+        if (wfull > w && ld_stream(cp + w * C) >= 0) {  // the row goes on past the cap: overflow
             V *op = ovf_part + (int64_t)ovf_id[i] * kMaxK;
 #pragma unroll
             for (int q = 0; q < K; q++) op[q] = s[q];
@@ -106,8 +105,13 @@ __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
     }
 }
 
-// piece = {overflow row, first element, end element} of the compact arrays;
-// one warp per piece, lanes on consecutive elements
+// Long tails (kPieceMin nonzeros or more) are cut into pieces of at most
+// kPieceElems nonzeros of one row, a warp per piece, lanes on consecutive
+// elements; piece = {overflow row, first element, end element} of the
+// compact arrays.
+constexpr int64_t kPieceMin = 1024;
+constexpr int64_t kPieceElems = 2048;
+
 template <typename V, int K>
 __global__ void __launch_bounds__(kBlock) sliced_piece_kernel(int64_t npieces, const int4 *__restrict__ pieces,
                                                               const int32_t *__restrict__ ocol,
@@ -148,46 +152,52 @@ __global__ void __launch_bounds__(kBlock) sliced_piece_kernel(int64_t npieces, c
     }
 }
 
-// one thread per overflow row: its thread partial plus its pieces, in order
+// One thread per overflow row o: its thread partial plus the rest of the row
+// -- the overflow CSR result y_ovf[o] (alpha = 1, beta = 0) for the first
+// nshort rows (short tails), the row's pieces in order for the others.
 template <typename V, int K>
-__global__ void sliced_piece_fixup(int64_t nov, const int32_t *__restrict__ ovf_rows,
-                                   const int32_t *__restrict__ piece_begin, const int32_t *__restrict__ reorder,
-                                   const V *__restrict__ ovf_part, const V *__restrict__ partial, V alpha, V beta,
-                                   V *__restrict__ y, int64_t ldy) {
+__global__ void sliced_overflow_fixup(int64_t nov, int64_t nshort, const int32_t *__restrict__ ovf_rows,
+                                      const int32_t *__restrict__ reorder, const V *__restrict__ ovf_part,
+                                      const V *__restrict__ y_ovf, const int32_t *__restrict__ piece_begin,
+                                      const V *__restrict__ partial, V alpha, V beta, V *__restrict__ y,
+                                      int64_t ldy) {
     const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= nov) return;
-    V s[K];
+    V sum[K];
 #pragma unroll
-    for (int q = 0; q < K; q++) s[q] = ovf_part[o * kMaxK + q];
-    for (int32_t p = piece_begin[o]; p < piece_begin[o + 1]; p++)
+    for (int q = 0; q < K; q++) sum[q] = ovf_part[o * kMaxK + q];
+    if (o < nshort) {
 #pragma unroll
-        for (int q = 0; q < K; q++) s[q] += partial[(int64_t)p * kMaxK + q];
+        for (int q = 0; q < K; q++) sum[q] += y_ovf[o * kMaxK + q];
+    } else {
+        for (int32_t pc = piece_begin[o - nshort]; pc < piece_begin[o - nshort + 1]; pc++)
+#pragma unroll
+            for (int q = 0; q < K; q++) sum[q] += partial[(int64_t)pc * kMaxK + q];
+    }
     const int64_t i = ovf_rows[o];
     const int64_t row = reorder ? (int64_t)reorder[i] : i;
     V *yp = y + row * ldy;
 #pragma unroll
-    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, s[q], beta, yp + q);
+    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, sum[q], beta, yp + q);
 }
 
-// Plan building: stored length of each row of a long chunk (padding is a
-// suffix: binary search for the first slot with col < 0).
-__global__ void long_row_lengths(int64_t ncand, int C, const int32_t *__restrict__ cand,
-                                 const int64_t *__restrict__ chunk_ptr, const int32_t *__restrict__ col,
-                                 int32_t *__restrict__ len) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ncand) return;
-    const int64_t i = cand[t];
-    const int64_t c = i / C;
-    const int r = (int)(i - c * C);
-    const int64_t base = chunk_ptr[c];
-    const int64_t w = (chunk_ptr[c + 1] - base) / C;
-    int64_t lo = 0, hi = w;  // first padding slot in [0, w]
-    while (lo < hi) {
-        const int64_t mid = (lo + hi) >> 1;
-        if (col[base + mid * C + r] >= 0) lo = mid + 1;
-        else hi = mid;
+// Plan building: stored length of every stored row (padding is a suffix:
+// binary search for the first slot with col < 0).
+__global__ void stored_row_lengths(int64_t m, int C, const int64_t *__restrict__ chunk_ptr,
+                                   const int32_t *__restrict__ col, int32_t *__restrict__ len) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = i / C;
+        const int r = (int)(i - c * C);
+        const int64_t base = chunk_ptr[c];
+        const int64_t w = (chunk_ptr[c + 1] - base) / C;
+        int64_t lo = 0, hi = w;  // first padding slot in [0, w]
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (col[base + mid * C + r] >= 0) lo = mid + 1;
+            else hi = mid;
+        }
+        len[i] = (int32_t)lo;
     }
-    len[t] = (int32_t)lo;
 }
 
 // Overflow ids of the stored rows: ovf_id[rows[o]] = o.
@@ -196,11 +206,11 @@ __global__ void set_overflow_ids(int64_t nov, const int32_t *__restrict__ rows, 
     if (o < nov) ovf_id[rows[o]] = (int32_t)o;
 }
 
-// Copies slots kLongWidth.. of each overflow row into the compact arrays
-// (one warp per row).
+// Copies slots cap.. of each overflow row into the compact CSR arrays (one
+// warp per row).
 template <typename V>
-__global__ void copy_overflow(int64_t nov, int C, const int32_t *__restrict__ ovf_rows,
-                              const int64_t *__restrict__ ovf_ptr, const int64_t *__restrict__ chunk_ptr,
+__global__ void copy_overflow(int64_t nov, int C, int64_t cap, const int32_t *__restrict__ ovf_rows,
+                              const int32_t *__restrict__ ovf_ptr, const int64_t *__restrict__ chunk_ptr,
                               const int32_t *__restrict__ col, const V *__restrict__ val, int32_t *__restrict__ ocol,
                               V *__restrict__ oval) {
     const int lane = threadIdx.x & 31;
@@ -209,8 +219,8 @@ __global__ void copy_overflow(int64_t nov, int C, const int32_t *__restrict__ ov
     const int64_t i = ovf_rows[o];
     const int64_t c = i / C;
     const int r = (int)(i - c * C);
-    const int64_t base = chunk_ptr[c] + kLongWidth * C + r;
-    const int64_t n = ovf_ptr[o + 1] - ovf_ptr[o], dst = ovf_ptr[o];
+    const int64_t base = chunk_ptr[c] + cap * C + r;
+    const int64_t n = (int64_t)ovf_ptr[o + 1] - ovf_ptr[o], dst = ovf_ptr[o];
     for (int64_t e = lane; e < n; e += 32) {
         ocol[dst + e] = col[base + e * C];
         oval[dst + e] = val[base + e * C];
@@ -225,99 +235,199 @@ struct SlicedView {
     const int32_t *col;
     const void *val;
     int64_t nchunks;
+    int64_t n;  // columns
 };
 
-// Overflow plan of a sliced matrix, built on its first SpMV: extra[0]
-// pieces (int4), extra[1] overflow rows (stored row positions), extra[2]
-// first piece of each overflow row (+1 entry), extra[3] piece partials,
-// extra[4] thread partials of the overflow rows, extra[5] / extra[6] compact
-// columns / values, extra[8] overflow id per stored row (-1: none);
-// extra_i[0] pieces, extra_i[1] overflow rows, extra_i[7] built.
-sspmv_status ensure_piece_plan(const sspmv_features *f, const SlicedView &v, Plan *p, sspmv_stream_t s) {
-    if (p->extra_i[7]) return SSPMV_OK;
-    std::lock_guard<std::mutex> g(plan_mutex());
-    if (p->extra_i[7]) return SSPMV_OK;
-    std::vector<int64_t> cp((size_t)v.nchunks + 1);
-    SSPMV_CUDA_TRY(cudaMemcpyAsync(cp.data(), v.chunk_ptr, cp.size() * 8, cudaMemcpyDeviceToHost, cu(s)));
-    SSPMV_CUDA_TRY(cudaStreamSynchronize(cu(s)));
-    std::vector<int32_t> cand;  // stored rows of long chunks
-    for (int64_t c = 0; c < v.nchunks; c++) {
-        const int64_t w = (cp[(size_t)c + 1] - cp[(size_t)c]) / v.C;
-        if (w <= kLongWidth) continue;
-        for (int r = 0; r < v.C && c * v.C + r < v.m; r++) cand.push_back((int32_t)(c * v.C + r));
+// Cost model of the cap, in picoseconds of GB300 time (fitted to measured
+// kernel times: the thread pass of S-ELL C=4 on a 4M-row power-law matrix,
+// the CSR stream kernel per nonzero on a 4M-row uniform matrix): the thread
+// pass costs kWarpSlotPs per warp and slot it runs (a warp runs as many slots
+// as its longest row, up to the cap), and no less than its longest thread:
+// kIterPs per 4 slots, each step a dependent chain of an HBM load and an x
+// gather (a 38k-slot row alone takes ~15 ms); the overflow costs kOvfNnzPs
+// per nonzero, kOvfRowPs per row (partial, CSR row, fix-up) and kOvfLaunchPs
+// for its extra launches.
+constexpr double kWarpSlotPs = 73.0;
+constexpr double kIterPs = 1.5e6;
+constexpr double kOvfNnzPs = 4.8;
+constexpr double kOvfRowPs = 20.0;
+constexpr double kOvfLaunchPs = 6.0e6;
+constexpr int64_t kCaps[] = {8, 12, 16, 24, 32, 48, 64, 96, 128, 256, 512};
+constexpr int64_t kNoCap = INT64_MAX;
+
+// The cap of least modelled time (kNoCap: no overflow), from the stored row
+// lengths (stored order: thread i runs stored row i, a warp 32 of them).
+int64_t choose_cap(const std::vector<int32_t> &len) {
+    const int64_t m = (int64_t)len.size();
+    constexpr int32_t H = 1024;  // exact histogram below H; longer rows listed
+    std::vector<int64_t> hist(H, 0);
+    std::vector<int32_t> longer, wmax((size_t)((m + 31) / 32), 0);
+    for (int64_t i = 0; i < m; i++) {
+        const int32_t l = len[(size_t)i];
+        int32_t &w = wmax[(size_t)(i >> 5)];
+        w = std::max(w, l);
+        if (l < H) hist[(size_t)l]++;
+        else longer.push_back(l);
     }
-    if (!cand.empty()) {
-        const size_t sv = vsize(f->value_type);
-        int32_t *dcand = nullptr, *dlen = nullptr;
-        SSPMV_TRY(dalloc(&dcand, cand.size(), s));
-        SSPMV_TRY(dalloc(&dlen, cand.size(), s));
-        SSPMV_CUDA_TRY(cudaMemcpyAsync(dcand, cand.data(), cand.size() * 4, cudaMemcpyHostToDevice, cu(s)));
-        long_row_lengths<<<grid_for((int64_t)cand.size(), 256), 256, 0, cu(s)>>>((int64_t)cand.size(), v.C, dcand,
-                                                                                v.chunk_ptr, v.col, dlen);
+    double slots = 0;
+    int32_t longest = 0;
+    for (int32_t w : wmax) {
+        slots += w;
+        longest = std::max(longest, w);
+    }
+    auto thread_pass = [&](double warp_slots, int64_t slots_of_longest) {
+        return std::max(kWarpSlotPs * warp_slots, kIterPs * (double)((slots_of_longest + 3) / 4));
+    };
+    double best_cost = thread_pass(slots, longest);
+    int64_t best = kNoCap;
+    for (int64_t cap : kCaps) {
+        double thread = 0, ovn = 0, ovr = 0;
+        for (int32_t w : wmax) thread += (double)std::min<int64_t>(w, cap);
+        for (int64_t l = cap + 1; l < H; l++) {
+            ovn += (double)hist[(size_t)l] * (double)(l - cap);
+            ovr += (double)hist[(size_t)l];
+        }
+        for (int32_t l : longer)
+            if (l > cap) {
+                ovn += (double)(l - cap);
+                ovr += 1;
+            }
+        const double cost = thread_pass(thread, std::min<int64_t>(longest, cap)) + kOvfNnzPs * ovn +
+                            kOvfRowPs * ovr + (ovr > 0 ? kOvfLaunchPs : 0.0);
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = cap;
+        }
+    }
+    return best;
+}
+
+void free_overflow(Plan *p, sspmv_stream_t s) {
+    if (p->sub) {
+        free_plan(&p->sub->f, s);
+        delete p->sub;
+        p->sub = nullptr;
+    }
+    for (int e : {0, 1, 2, 3, 4, 5, 6, 7, 8, 9}) {
+        dfree(p->extra[e], s);
+        p->extra[e] = nullptr;
+    }
+    p->extra_i[1] = p->extra_i[4] = p->extra_i[5] = 0;
+}
+
+// Overflow plan of a sliced matrix, built on its first SpMV (and again after
+// sspmv_set_kernel changes the cap).  Overflow rows are ordered short tails
+// first, then long tails (kPieceMin nonzeros or more), their tails copied in
+// that order into the compact arrays.  extra[0] compact row offsets (nov+1;
+// its first nshort+1 entries are the short-tail CSR's row_offset), extra[1]
+// overflow rows (stored positions), extra[2] short-tail CSR result (nshort x
+// kMaxK), extra[3] pieces (int4), extra[4] thread partials of the overflow
+// rows, extra[5] / extra[6] compact columns / values, extra[7] piece partials,
+// extra[8] overflow id per stored row (-1: none), extra[9] first piece of each
+// long row (+1 entry); p->sub the short-tail CSR matrix (its stream plan built
+// here); extra_i[1] overflow rows, [2] the cap, [3] the kernel parameter the
+// plan was built for, [4] short-tail rows, [5] pieces, [7] built.
+sspmv_status ensure_overflow_plan(const sspmv_features *f, const SlicedView &v, Plan *p, sspmv_stream_t s) {
+    if (p->extra_i[7] && p->extra_i[3] == p->param) return SSPMV_OK;
+    std::lock_guard<PlanMutex> g(plan_mutex());
+    if (p->extra_i[7] && p->extra_i[3] == p->param) return SSPMV_OK;
+    p->extra_i[7] = 0;
+    free_overflow(p, s);  // a plan for another cap, or one whose building failed
+    std::vector<int32_t> len((size_t)v.m);
+    {
+        int32_t *dlen = nullptr;
+        SSPMV_TRY(dalloc(&dlen, (size_t)v.m, s));
+        stored_row_lengths<<<grid_for(v.m, 256, (int64_t)num_sms() * 32), 256, 0, cu(s)>>>(v.m, v.C, v.chunk_ptr,
+                                                                                           v.col, dlen);
         SSPMV_LAUNCH_CHECK();
-        std::vector<int32_t> len(cand.size());
         SSPMV_CUDA_TRY(cudaMemcpyAsync(len.data(), dlen, len.size() * 4, cudaMemcpyDeviceToHost, cu(s)));
         SSPMV_CUDA_TRY(cudaStreamSynchronize(cu(s)));
-        dfree(dcand, s);
         dfree(dlen, s);
-        std::vector<int32_t> rows, begin;
-        std::vector<int64_t> optr{0};
-        std::vector<int4> pieces;
-        for (size_t t = 0; t < cand.size(); t++) {
-            if (len[t] <= kLongWidth) continue;
-            const int64_t n = len[t] - kLongWidth, o0 = optr.back();
-            if (o0 + n > 0x7fffffff) return fail(SSPMV_NOT_SUPPORTED, "long-row overflow exceeds the int32 range");
-            rows.push_back(cand[t]);
-            begin.push_back((int32_t)pieces.size());
-            for (int64_t e = 0; e < n; e += kPieceElems)
-                pieces.push_back(make_int4((int)rows.size() - 1, (int)(o0 + e), (int)(o0 + std::min(n, e + kPieceElems)),
-                                           0));
-            optr.push_back(o0 + n);
-        }
-        begin.push_back((int32_t)pieces.size());
-        const int64_t nov = (int64_t)rows.size(), novf = optr.back();
-        if (nov > 0) {
-            int4 *dp = nullptr;
-            int32_t *drows = nullptr, *db = nullptr, *dov = nullptr, *ocol = nullptr;
-            int64_t *dptr = nullptr;
-            unsigned char *part = nullptr, *opart = nullptr, *oval = nullptr;
-            SSPMV_TRY(dalloc(&dp, pieces.size(), s));
-            SSPMV_TRY(dalloc(&drows, rows.size(), s));
-            SSPMV_TRY(dalloc(&db, begin.size(), s));
-            SSPMV_TRY(dalloc(&dptr, optr.size(), s));
-            SSPMV_TRY(dalloc(&part, pieces.size() * kMaxK * sv, s));
-            SSPMV_TRY(dalloc(&opart, (size_t)nov * kMaxK * sv, s));
-            SSPMV_TRY(dalloc(&ocol, (size_t)novf, s));
-            SSPMV_TRY(dalloc(&oval, (size_t)novf * sv, s));
-            SSPMV_TRY(dalloc(&dov, (size_t)v.m, s));
-            SSPMV_CUDA_TRY(cudaMemcpyAsync(dp, pieces.data(), pieces.size() * sizeof(int4), cudaMemcpyHostToDevice, cu(s)));
-            SSPMV_CUDA_TRY(cudaMemcpyAsync(drows, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice, cu(s)));
-            SSPMV_CUDA_TRY(cudaMemcpyAsync(db, begin.data(), begin.size() * 4, cudaMemcpyHostToDevice, cu(s)));
-            SSPMV_CUDA_TRY(cudaMemcpyAsync(dptr, optr.data(), optr.size() * 8, cudaMemcpyHostToDevice, cu(s)));
-            SSPMV_CUDA_TRY(cudaMemsetAsync(dov, 0xff, (size_t)v.m * 4, cu(s)));
-            set_overflow_ids<<<grid_for(nov, 256), 256, 0, cu(s)>>>(nov, drows, dov);
-            SSPMV_LAUNCH_CHECK();
-            SSPMV_TRY(dispatch_value(f->value_type, [&](auto tag) -> sspmv_status {
-                using V = decltype(tag);
-                copy_overflow<V><<<grid_for(nov * 32, 256), 256, 0, cu(s)>>>(nov, v.C, drows, dptr, v.chunk_ptr, v.col,
-                                                                             (const V *)v.val, ocol, (V *)oval);
-                SSPMV_LAUNCH_CHECK();
-                return SSPMV_OK;
-            }));
-            SSPMV_CUDA_TRY(cudaStreamSynchronize(cu(s)));
-            dfree(dptr, s);
-            p->extra[0] = dp;
-            p->extra[1] = drows;
-            p->extra[2] = db;
-            p->extra[3] = part;
-            p->extra[4] = opart;
-            p->extra[5] = ocol;
-            p->extra[6] = oval;
-            p->extra[8] = dov;
-            p->extra_i[0] = (int64_t)pieces.size();
-            p->extra_i[1] = nov;
-        }
     }
+    const int64_t cap = p->param > 0 ? (int64_t)p->param : choose_cap(len);
+    std::vector<int32_t> rows, long_rows;
+    int64_t total = 0;
+    for (int64_t i = 0; i < v.m; i++) {
+        const int64_t l = len[(size_t)i];
+        if (l <= cap) continue;
+        total += l - cap;
+        (l - cap >= kPieceMin ? long_rows : rows).push_back((int32_t)i);
+    }
+    if (total > 0x7fffffff) return fail(SSPMV_NOT_SUPPORTED, "overflow of the long rows exceeds the int32 range");
+    const int64_t nshort = (int64_t)rows.size();
+    rows.insert(rows.end(), long_rows.begin(), long_rows.end());
+    const int64_t nov = (int64_t)rows.size();
+    std::vector<int32_t> optr{0}, pbegin;
+    std::vector<int4> pieces;
+    for (int64_t o = 0; o < nov; o++) {
+        const int32_t o0 = optr.back(), n = len[(size_t)rows[(size_t)o]] - (int32_t)cap;
+        if (o >= nshort) {
+            pbegin.push_back((int32_t)pieces.size());
+            for (int64_t e = 0; e < n; e += kPieceElems)
+                pieces.push_back(make_int4((int)o, (int)(o0 + e), (int)(o0 + std::min<int64_t>(n, e + kPieceElems)), 0));
+        }
+        optr.push_back(o0 + n);
+    }
+    pbegin.push_back((int32_t)pieces.size());
+    const int64_t novf = optr.back(), npieces = (int64_t)pieces.size();
+    if (nov > 0) {
+        const size_t sv = vsize(f->value_type);
+        int32_t *dptr = nullptr, *drows = nullptr, *dov = nullptr, *ocol = nullptr, *dpb = nullptr;
+        int4 *dpieces = nullptr;
+        unsigned char *yov = nullptr, *opart = nullptr, *oval = nullptr, *ppart = nullptr;
+        // each buffer belongs to the plan as soon as it exists (free_overflow)
+        SSPMV_TRY(dalloc(&dptr, optr.size(), s));
+        p->extra[0] = dptr;
+        SSPMV_TRY(dalloc(&drows, rows.size(), s));
+        p->extra[1] = drows;
+        SSPMV_TRY(dalloc(&yov, (size_t)std::max<int64_t>(nshort, 1) * kMaxK * sv, s));
+        p->extra[2] = yov;
+        SSPMV_TRY(dalloc(&dpieces, pieces.size(), s));
+        p->extra[3] = dpieces;
+        SSPMV_TRY(dalloc(&opart, (size_t)nov * kMaxK * sv, s));
+        p->extra[4] = opart;
+        SSPMV_TRY(dalloc(&ocol, (size_t)novf, s));
+        p->extra[5] = ocol;
+        SSPMV_TRY(dalloc(&oval, (size_t)novf * sv, s));
+        p->extra[6] = oval;
+        SSPMV_TRY(dalloc(&ppart, (size_t)std::max<int64_t>(npieces, 1) * kMaxK * sv, s));
+        p->extra[7] = ppart;
+        SSPMV_TRY(dalloc(&dov, (size_t)v.m, s));
+        p->extra[8] = dov;
+        SSPMV_TRY(dalloc(&dpb, pbegin.size(), s));
+        p->extra[9] = dpb;
+        SSPMV_CUDA_TRY(cudaMemcpyAsync(dptr, optr.data(), optr.size() * 4, cudaMemcpyHostToDevice, cu(s)));
+        SSPMV_CUDA_TRY(cudaMemcpyAsync(drows, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice, cu(s)));
+        SSPMV_CUDA_TRY(cudaMemcpyAsync(dpb, pbegin.data(), pbegin.size() * 4, cudaMemcpyHostToDevice, cu(s)));
+        if (npieces > 0)
+            SSPMV_CUDA_TRY(cudaMemcpyAsync(dpieces, pieces.data(), pieces.size() * sizeof(int4),
+                                           cudaMemcpyHostToDevice, cu(s)));
+        SSPMV_CUDA_TRY(cudaMemsetAsync(dov, 0xff, (size_t)v.m * 4, cu(s)));
+        set_overflow_ids<<<grid_for(nov, 256), 256, 0, cu(s)>>>(nov, drows, dov);
+        SSPMV_LAUNCH_CHECK();
+        SSPMV_TRY(dispatch_value(f->value_type, [&](auto tag) -> sspmv_status {
+            using V = decltype(tag);
+            copy_overflow<V><<<grid_for(nov * 32, 256), 256, 0, cu(s)>>>(nov, v.C, cap, drows, dptr, v.chunk_ptr,
+                                                                         v.col, (const V *)v.val, ocol, (V *)oval);
+            SSPMV_LAUNCH_CHECK();
+            return SSPMV_OK;
+        }));
+        if (nshort > 0) {
+            p->sub = new (std::nothrow) sspmv_csr();
+            if (!p->sub) return fail(SSPMV_OUT_OF_MEMORY, "overflow matrix allocation failed");
+            SSPMV_TRY(sspmv_csr_wrap(p->sub, f->value_type, nshort, v.n, optr[(size_t)nshort], dptr, ocol, oval));
+            const int32_t *rs = nullptr;
+            int64_t nch = 0;
+            int32_t gap = 0;
+            SSPMV_TRY(csr_stream_plan(p->sub, &rs, &nch, &gap, s));  // built now, not inside a later SpMV
+        }
+        SSPMV_CUDA_TRY(cudaStreamSynchronize(cu(s)));
+    }
+    p->extra_i[1] = nov;
+    p->extra_i[2] = nov > 0 ? cap : kNoCap;
+    p->extra_i[3] = p->param;
+    p->extra_i[4] = nshort;
+    p->extra_i[5] = npieces;
     p->extra_i[7] = 1;
     return SSPMV_OK;
 }
@@ -329,18 +439,21 @@ sspmv_status launch_sliced(const SlicedView &v, Plan *p, V alpha, const V *x, in
     const unsigned grid = grid_for(v.m, kBlock, (int64_t)num_sms() * 16);
     sliced_spmv_kernel<V, K><<<grid, kBlock, 0, cu(s)>>>(
         (int)v.m, v.C, v.chunk_ptr, v.reorder, v.col, (const V *)v.val, x, ldx, alpha, beta, y, ldy,
-        nov > 0 ? kLongWidth : INT64_MAX, nov > 0 ? (const int32_t *)p->extra[8] : nullptr,
+        nov > 0 ? p->extra_i[2] : kNoCap, nov > 0 ? (const int32_t *)p->extra[8] : nullptr,
         nov > 0 ? (V *)p->extra[4] : nullptr);
     SSPMV_LAUNCH_CHECK();
     if (nov > 0) {
-        const int64_t npieces = p->extra_i[0];
-        sliced_piece_kernel<V, K><<<grid_for(npieces * 32, kBlock), kBlock, 0, cu(s)>>>(
-            npieces, (const int4 *)p->extra[0], (const int32_t *)p->extra[5], (const V *)p->extra[6], x, ldx,
-            (V *)p->extra[3]);
-        SSPMV_LAUNCH_CHECK();
-        sliced_piece_fixup<V, K><<<grid_for(nov, 256), 256, 0, cu(s)>>>(
-            nov, (const int32_t *)p->extra[1], (const int32_t *)p->extra[2], v.reorder, (const V *)p->extra[4],
-            (const V *)p->extra[3], alpha, beta, y, ldy);
+        const int64_t nshort = p->extra_i[4], npieces = p->extra_i[5];
+        if (nshort > 0) SSPMV_TRY(sspmv_spmm_csr(1.0, p->sub, K, x, ldx, 0.0, p->extra[2], kMaxK, s));
+        if (npieces > 0) {
+            sliced_piece_kernel<V, K><<<grid_for(npieces * 32, kBlock), kBlock, 0, cu(s)>>>(
+                npieces, (const int4 *)p->extra[3], (const int32_t *)p->extra[5], (const V *)p->extra[6], x, ldx,
+                (V *)p->extra[7]);
+            SSPMV_LAUNCH_CHECK();
+        }
+        sliced_overflow_fixup<V, K><<<grid_for(nov, 256), 256, 0, cu(s)>>>(
+            nov, nshort, (const int32_t *)p->extra[1], v.reorder, (const V *)p->extra[4], (const V *)p->extra[2],
+            (const int32_t *)p->extra[9], (const V *)p->extra[7], alpha, beta, y, ldy);
         SSPMV_LAUNCH_CHECK();
     }
     return SSPMV_OK;
@@ -351,10 +464,10 @@ sspmv_status spmm_sliced(const sspmv_features *f, const SlicedView &v, double al
     SSPMV_TRY(check_spmm_args(f, k, X, ldx, Y, ldy));
     if (v.m == 0) return SSPMV_OK;
     Plan *p = nullptr;
-    if (v.nchunks > 0) {  // ELL (nchunks == 0 here) has no pieces
+    if (v.nchunks > 0) {  // ELL (nchunks == 0 here) keeps every row in the thread pass
         p = get_plan(f);
         if (!p) return fail(SSPMV_OUT_OF_MEMORY, "plan allocation failed");
-        SSPMV_TRY(ensure_piece_plan(f, v, p, s));
+        SSPMV_TRY(ensure_overflow_plan(f, v, p, s));
     }
     return dispatch_value(f->value_type, [&](auto tag) -> sspmv_status {
         using V = decltype(tag);
@@ -621,7 +734,7 @@ extern "C" sspmv_status sspmv_spmm_ell(double alpha, const sspmv_ell *A, int32_t
     if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
     Plan *p = get_plan(&A->f);
     SlicedView v{A->f.num_rows, (int32_t)std::max<int64_t>(A->f.num_rows, 1), (const int64_t *)p->extra[0], nullptr,
-                 A->col_index, A->values, 0};
+                 A->col_index, A->values, 0, A->f.num_cols};
     return spmm_sliced(&A->f, v, alpha, k, X, ldx, beta, Y, ldy, s);
 }
 
@@ -695,7 +808,8 @@ extern "C" sspmv_status sspmv_csr_to_sell(const sspmv_csr *csr, int32_t C, int32
 extern "C" sspmv_status sspmv_spmm_sell(double alpha, const sspmv_s_ell *A, int32_t k, const void *X, int64_t ldx,
                                         double beta, void *Y, int64_t ldy, sspmv_stream_t s) {
     if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
-    SlicedView v{A->f.num_rows, A->sliceWidth, A->chunk_ptr, nullptr, A->col_index, A->values, A->chunk_num};
+    SlicedView v{A->f.num_rows, A->sliceWidth,   A->chunk_ptr,   nullptr,
+                 A->col_index,  A->values,     A->chunk_num,   A->f.num_cols};
     return spmm_sliced(&A->f, v, alpha, k, X, ldx, beta, Y, ldy, s);
 }
 
@@ -768,7 +882,8 @@ extern "C" sspmv_status sspmv_csr_to_sell_c_sigma(const sspmv_csr *csr, int32_t 
 extern "C" sspmv_status sspmv_spmm_sell_c_sigma(double alpha, const sspmv_sell_c_sigma *A, int32_t k, const void *X,
                                                 int64_t ldx, double beta, void *Y, int64_t ldy, sspmv_stream_t s) {
     if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
-    SlicedView v{A->f.num_rows, A->chunkWidth_C, A->chunk_ptr, A->reorder, A->col_index, A->values, A->validchunkNum};
+    SlicedView v{A->f.num_rows, A->chunkWidth_C,   A->chunk_ptr,   A->reorder,
+                 A->col_index,  A->values,         A->validchunkNum, A->f.num_cols};
     return spmm_sliced(&A->f, v, alpha, k, X, ldx, beta, Y, ldy, s);
 }
 
@@ -836,7 +951,8 @@ extern "C" sspmv_status sspmv_csr_to_sell_c_R(const sspmv_csr *csr, int32_t C, i
 extern "C" sspmv_status sspmv_spmm_sell_c_R(double alpha, const sspmv_sell_c_R *A, int32_t k, const void *X,
                                             int64_t ldx, double beta, void *Y, int64_t ldy, sspmv_stream_t s) {
     if (!A) return fail(SSPMV_INVALID_ARG, "null matrix");
-    SlicedView v{A->f.num_rows, A->chunkWidth_C, A->chunk_ptr, A->reorder, A->col_index, A->values, A->validchunkNum};
+    SlicedView v{A->f.num_rows, A->chunkWidth_C,   A->chunk_ptr,   A->reorder,
+                 A->col_index,  A->values,         A->validchunkNum, A->f.num_cols};
     return spmm_sliced(&A->f, v, alpha, k, X, ldx, beta, Y, ldy, s);
 }
 

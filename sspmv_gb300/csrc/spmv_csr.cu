@@ -237,27 +237,21 @@ __global__ void csr_merge_fixup(int64_t num_tiles, int m, const int32_t *__restr
                                 const int32_t *__restrict__ has_end, const V *__restrict__ carry_val,
                                 const V *__restrict__ head_val, V alpha, V beta, V *__restrict__ y,
                                 int64_t ldy) {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= num_tiles) return;
-    const int r = carry_row[t];
-    if (r >= m) return;
-    const int rs = row_offset[r];
-    if (rs < coords[t].y || rs >= coords[t + 1].y) return;
-    V tot[K];
-#pragma unroll
-    for (int q = 0; q < K; q++) tot[q] = carry_val[t * kMaxK + q];
-    for (int64_t u = t + 1; u < num_tiles; u++) {
-        if (has_end[u]) {
-#pragma unroll
-            for (int q = 0; q < K; q++) tot[q] += head_val[u * kMaxK + q];
-            break;
-        }
-#pragma unroll
-        for (int q = 0; q < K; q++) tot[q] += carry_val[u * kMaxK + q];
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t - (threadIdx.x & 31) >= num_tiles) return;  // whole warp past the end
+    const int r = t < num_tiles ? carry_row[t] : m;
+    bool mine = false;
+    if (r < m) {
+        const int rs = row_offset[r];
+        mine = rs >= coords[t].y && rs < coords[t + 1].y;  // the row starts in tile t
     }
-    V *yp = y + (int64_t)r * ldy;
+    V tot[K];
+    chain_sum<V, K>(mine, t, num_tiles, 0, has_end, carry_val, head_val, tot);
+    if (mine) {
+        V *yp = y + (int64_t)r * ldy;
 #pragma unroll
-    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
+        for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
+    }
 }
 
 template <typename V, int K, int VS>
@@ -720,6 +714,138 @@ __device__ __forceinline__ void stream_chunk_lanes(
     }
 }
 
+// The chunk of a matrix without empty rows whose nonzeros lie in at most
+// kFastRows + 1 rows (a warp-uniform test): lane j reads rp[ra + j] once, and
+// each lane finds the row of its first nonzero and the ends of the next
+// eight rows by shuffles -- no chain of dependent loads on row_offset.  The
+// arithmetic (per-lane sums in nonzero order, the segmented scan, the carry
+// slots) is that of stream_chunk_lanes, so both give the same bits.
+constexpr int kFastRows = 32 - kStreamPerLane - 1;
+
+template <typename V, int K>
+__device__ __forceinline__ void stream_chunk_fast(
+    int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
+    const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy, const int ra,
+    const int64_t w, const int64_t slot, int32_t *__restrict__ carry_row, int32_t *__restrict__ has_end,
+    V *__restrict__ carry_val, V *__restrict__ head_val, int vec) {
+    constexpr unsigned kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int64_t j0 = w * kStreamChunk;
+    const int64_t j1 = min(j0 + (int64_t)kStreamChunk, nnz);
+    const int64_t e0 = j0 + (int64_t)lane * kStreamPerLane;
+    const int nv = (int)max((int64_t)0, min((int64_t)kStreamPerLane, j1 - e0));
+    int c[8];
+    V a[8];
+    stream_load8<V>(ci, cv, e0, nv, vec != 0, c, a);
+    // R_j = rp[ra + j]: the starts of rows ra .. ra + 31 (past the end: never <= e0)
+    const int rl = ra + lane <= m ? __ldg(rp + ra + lane) : 0x7fffffff;
+    const bool head_open = __shfl_sync(kFull, rl, 0) < j0;  // the chunk's first row began in an earlier chunk
+    // largest p with R_p <= e0 (R_0 <= j0 <= e0): the lane's first row is ra + p
+    int pos = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+        const int v = __shfl_sync(kFull, rl, (pos + step) & 31);
+        if (pos + step <= 31 && (int64_t)v <= e0) pos += step;
+    }
+    // bit u of `ends`: the lane's nonzero u is the last of its row (row ends
+    // R_{pos+1} .. R_{pos+8} that fall on e0+1 .. e0+8)
+    uint32_t ends = 0;
+#pragma unroll
+    for (int k = 1; k <= kStreamPerLane; k++) {
+        const int v = __shfl_sync(kFull, rl, (pos + k) & 31);
+        const int64_t u = (int64_t)v - 1 - e0;
+        if (pos + k <= 31 && u >= 0 && u < kStreamPerLane) ends |= 1u << u;
+    }
+    V xv[K <= 2 ? 8 : 1][K];
+    if constexpr (K <= 2) {
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int q = 0; q < K; q++) xv[u][q] = u < nv ? ld_x(x + (int64_t)c[u] * ldx + q) : V(0);
+    }
+    int r = ra + pos;
+    V seg[K], head[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) seg[q] = head[q] = V(0);
+    bool any_end = false, last_open = false;
+    int head_row = -1, last_row = -1;
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+        if (u < nv) {
+#pragma unroll
+            for (int q = 0; q < K; q++) {
+                if constexpr (K <= 2) seg[q] += a[u] * xv[u][q];
+                else seg[q] += a[u] * ld_x(x + (int64_t)c[u] * ldx + q);
+            }
+            last_row = r;
+            last_open = !((ends >> u) & 1u);
+            if (!last_open) {  // row r ends here
+                if (!any_end) {
+                    any_end = true;
+                    head_row = r;
+#pragma unroll
+                    for (int q = 0; q < K; q++) head[q] = seg[q];
+                } else {
+                    V *yp = y + (int64_t)r * ldy;
+#pragma unroll
+                    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, seg[q], beta, yp + q);
+                }
+#pragma unroll
+                for (int q = 0; q < K; q++) seg[q] = V(0);
+                r++;
+            }
+        }
+    }
+    V S[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) S[q] = seg[q];
+    bool f = any_end;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        V up[K];
+#pragma unroll
+        for (int q = 0; q < K; q++) up[q] = __shfl_up_sync(kFull, S[q], o);
+        const bool fu = __shfl_up_sync(kFull, f, o);
+        if (lane >= o) {
+            if (!f) {
+#pragma unroll
+                for (int q = 0; q < K; q++) S[q] += up[q];
+            }
+            f = f || fu;
+        }
+    }
+    V cin[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        cin[q] = __shfl_up_sync(kFull, S[q], 1);
+        if (lane == 0) cin[q] = V(0);
+    }
+    if (any_end) {
+        V tot[K];
+#pragma unroll
+        for (int q = 0; q < K; q++) tot[q] = head[q] + cin[q];
+        if (head_row == ra && head_open) {
+            V *hp = head_val + slot * kMaxK;
+#pragma unroll
+            for (int q = 0; q < K; q++) hp[q] = tot[q];
+        } else {
+            V *yp = y + (int64_t)head_row * ldy;
+#pragma unroll
+            for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
+        }
+    }
+    const bool chunk_end = __any_sync(kFull, any_end);
+    if (nv > 0 && e0 + nv == j1) {  // the lane holding the chunk's last nonzero
+        has_end[slot] = chunk_end ? 1 : 0;
+        carry_row[slot] = last_open ? last_row : -1;
+        if (last_open) {
+            V *cp = carry_val + slot * kMaxK;
+#pragma unroll
+            for (int q = 0; q < K; q++) cp[q] = S[q];
+        }
+    }
+}
+
 // One lane per nonzero run (stream_chunk_lanes), except FP64 with k = 8:
 // column groups (stream_chunk_cols), which read each 64-byte row of X with
 // one coalesced access (measured 1.3-1.4x faster there; slower for FP32 and
@@ -729,13 +855,22 @@ __device__ __forceinline__ void stream_chunk(
     int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
     const int32_t *__restrict__ row_start, const int64_t w, const int64_t slot, int32_t *__restrict__ carry_row,
-    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val, int vec) {
-    if constexpr (K == 8 && sizeof(V) == 8)
+    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val, int vec, int no_empty) {
+    if constexpr (K == 8 && sizeof(V) == 8) {
         stream_chunk_cols<V, K, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, slot, carry_row,
                                    has_end, carry_val, head_val);
-    else
+    } else {
+        if (no_empty && w * kStreamChunk < nnz) {  // warp-uniform
+            const int ra = __ldg(row_start + w);
+            if (min(__ldg(row_start + w + 1), m - 1) - ra <= kFastRows) {
+                stream_chunk_fast<V, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, ra, w, slot, carry_row,
+                                        has_end, carry_val, head_val, vec);
+                return;
+            }
+        }
         stream_chunk_lanes<V, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, slot, carry_row,
                                  has_end, carry_val, head_val, vec);
+    }
 }
 
 template <typename V, int K>
@@ -743,37 +878,29 @@ __global__ void __launch_bounds__(kBlock) csr_stream_kernel(
     int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
     const int32_t *__restrict__ row_start, int32_t *__restrict__ carry_row, int32_t *__restrict__ has_end,
-    V *__restrict__ carry_val, V *__restrict__ head_val, int vec) {
+    V *__restrict__ carry_val, V *__restrict__ head_val, int vec, int no_empty) {
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     stream_chunk<V, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, w, carry_row, has_end,
-                       carry_val, head_val, vec);
+                       carry_val, head_val, vec, no_empty);
 }
 
-// Rows crossing chunks: the chunk where the row starts adds the later
-// chunks' pieces in order.
+// Rows crossing chunks: a thread per chunk; the chunk where the row starts
+// adds the later chunks' pieces (chain_sum).
 template <typename V, int K>
 __global__ void csr_stream_fixup(int64_t nt, const int32_t *__restrict__ rp, const int32_t *__restrict__ carry_row,
                                  const int32_t *__restrict__ has_end, const V *__restrict__ carry_val,
                                  const V *__restrict__ head_val, V alpha, V beta, V *__restrict__ y, int64_t ldy) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nt) return;
-    const int r = carry_row[t];
-    if (r < 0 || (int64_t)rp[r] < t * kStreamChunk) return;  // not open here, or began in an earlier chunk
+    if (t - (threadIdx.x & 31) >= nt) return;  // whole warp past the end
+    const int r = t < nt ? carry_row[t] : -1;
+    const bool mine = r >= 0 && (int64_t)rp[r] >= t * kStreamChunk;  // open here and began here
     V tot[K];
+    chain_sum<V, K>(mine, t, nt, 0, has_end, carry_val, head_val, tot);
+    if (mine) {
+        V *yp = y + (int64_t)r * ldy;
 #pragma unroll
-    for (int q = 0; q < K; q++) tot[q] = carry_val[t * kMaxK + q];
-    for (int64_t u = t + 1; u < nt; u++) {
-        if (has_end[u]) {
-#pragma unroll
-            for (int q = 0; q < K; q++) tot[q] += head_val[u * kMaxK + q];
-            break;
-        }
-#pragma unroll
-        for (int q = 0; q < K; q++) tot[q] += carry_val[u * kMaxK + q];
+        for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
     }
-    V *yp = y + (int64_t)r * ldy;
-#pragma unroll
-    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
 }
 
 // Plan slots of the stream kernel (CSR matrices use no other extra slots):
@@ -782,7 +909,7 @@ __global__ void csr_stream_fixup(int64_t nt, const int32_t *__restrict__ rp, con
 // empty-row run (capped just above kStreamMaxGap).
 sspmv_status ensure_stream_plan(const sspmv_csr *A, Plan *p, sspmv_stream_t s) {
     if (p->extra[0]) return SSPMV_OK;
-    std::lock_guard<std::mutex> g(plan_mutex());
+    std::lock_guard<PlanMutex> g(plan_mutex());
     if (p->extra[0]) return SSPMV_OK;
     const int64_t m = A->f.num_rows, nnz = A->f.num_nnzs;
     const int64_t nt = std::max<int64_t>((nnz + kStreamChunk - 1) / kStreamChunk, 1);
@@ -824,7 +951,8 @@ sspmv_status launch_stream(const sspmv_csr *A, Plan *p, V alpha, const V *x, int
     const int vec = ((reinterpret_cast<uintptr_t>(A->col_index) | reinterpret_cast<uintptr_t>(A->values)) & 15) == 0;
     csr_stream_kernel<V, K><<<grid_for(nt * 32, kBlock), kBlock, 0, cu(s)>>>(
         (int)A->f.num_rows, A->f.num_nnzs, A->row_offset, A->col_index, (const V *)A->values, x, ldx, alpha, beta,
-        y, ldy, (const int32_t *)p->extra[0], ints, ints + nt, (V *)p->extra[2], (V *)p->extra[3], vec);
+        y, ldy, (const int32_t *)p->extra[0], ints, ints + nt, (V *)p->extra[2], (V *)p->extra[3], vec,
+        p->extra_i[1] == 0 ? 1 : 0);
     SSPMV_LAUNCH_CHECK();
     if (nt > 1) {
         csr_stream_fixup<V, K><<<grid_for(nt, 256), 256, 0, cu(s)>>>(nt, A->row_offset, ints, ints + nt,
@@ -868,7 +996,7 @@ __global__ void __launch_bounds__(kBlock) csr_batch_kernel(int g, const BatchHea
         const BatchItem *q = items + batch_item_of(items, n, gc);
         stream_chunk<V, K>(q->m, q->nnz, q->row_offset, q->col_index, (const V *)q->values, (const V *)q->x, q->ldx,
                            (V)q->alpha, (V)q->beta, (V *)q->y, q->ldy, q->row_start, gc - q->chunk_begin, base + gc,
-                           carry_row, has_end, carry_val, head_val, q->vec);
+                           carry_row, has_end, carry_val, head_val, q->vec, 0);
     }
 }
 
@@ -881,31 +1009,25 @@ __global__ void csr_batch_fixup(int g, const BatchHeader *__restrict__ hdr, cons
     const int64_t total = hdr->total_chunks[g];
     const int64_t base = hdr->carry_base[g];
     const BatchItem *items = all_items + hdr->item_begin[g];
-    for (int64_t gc = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gc < total;
-         gc += (int64_t)gridDim.x * blockDim.x) {
-        const BatchItem *q = items + batch_item_of(items, n, gc);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    // warp-uniform trip count: lane l takes global chunk w0 + l of each round
+    for (int64_t w0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane; w0 < total; w0 += stride) {
+        const int64_t gc = w0 + lane;
+        const BatchItem *q = gc < total ? items + batch_item_of(items, n, gc) : items;
         const int64_t t = gc - q->chunk_begin, nt = q->num_chunks;
-        if (nt <= 1) continue;
         const int64_t slot = base + gc;
-        const int r = carry_row[slot];
-        if (r < 0 || (int64_t)q->row_offset[r] < t * kStreamChunk) continue;
+        const int r = gc < total && nt > 1 ? carry_row[slot] : -1;
+        const bool mine = r >= 0 && (int64_t)q->row_offset[r] >= t * kStreamChunk;
         V tot[K];
+        const int64_t shift = slot - t;  // chunk u of this lane's item lives in slot u + shift
+        chain_sum<V, K>(mine, t, nt, shift, has_end, carry_val, head_val, tot);
+        if (mine) {
+            V *yp = (V *)q->y + (int64_t)r * q->ldy;
+            const V alpha = (V)q->alpha, beta = (V)q->beta;
 #pragma unroll
-        for (int c = 0; c < K; c++) tot[c] = carry_val[slot * kMaxK + c];
-        for (int64_t u = t + 1; u < nt; u++) {
-            const int64_t su = slot + (u - t);
-            if (has_end[su]) {
-#pragma unroll
-                for (int c = 0; c < K; c++) tot[c] += head_val[su * kMaxK + c];
-                break;
-            }
-#pragma unroll
-            for (int c = 0; c < K; c++) tot[c] += carry_val[su * kMaxK + c];
+            for (int c = 0; c < K; c++) yp[c] = axpby(alpha, tot[c], beta, yp + c);
         }
-        V *yp = (V *)q->y + (int64_t)r * q->ldy;
-        const V alpha = (V)q->alpha, beta = (V)q->beta;
-#pragma unroll
-        for (int c = 0; c < K; c++) yp[c] = axpby(alpha, tot[c], beta, yp + c);
     }
 }
 
@@ -934,7 +1056,7 @@ sspmv_status launch_batch_vk(int g, const BatchHeader *hdr, const BatchItem *ite
     const unsigned grid = (unsigned)(num_sms() * batch_blocks_per_sm<V, K>());
     csr_batch_kernel<V, K><<<grid, kBlock, 0, cu(s)>>>(g, hdr, items, carry_row, has_end, carry_val, head_val);
     SSPMV_LAUNCH_CHECK();
-    csr_batch_fixup<V, K><<<(unsigned)num_sms() * 2, 256, 0, cu(s)>>>(g, hdr, items, carry_row, has_end, carry_val,
+    csr_batch_fixup<V, K><<<(unsigned)num_sms() * 4, 256, 0, cu(s)>>>(g, hdr, items, carry_row, has_end, carry_val,
                                                                         head_val);
     SSPMV_LAUNCH_CHECK();
     return SSPMV_OK;
@@ -986,7 +1108,7 @@ sspmv_status ensure_merge_plan(Plan *p, int which, int64_t m, int64_t nnz, const
                                int32_t value_type, sspmv_stream_t s) {
     MergePlan &mp = p->merge[which];
     if (mp.coords) return SSPMV_OK;
-    std::lock_guard<std::mutex> g(plan_mutex());
+    std::lock_guard<PlanMutex> g(plan_mutex());
     if (mp.coords) return SSPMV_OK;
     const int tile = which == 0 ? MergeShape<1>::tile : MergeShape<8>::tile;
     const int64_t tiles = (m + nnz + tile - 1) / tile;

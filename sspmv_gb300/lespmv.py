@@ -332,6 +332,16 @@ def grx_features(csr: CSR_Matrix, tile_blocks: int = 256, group: int = 0, stream
     return out
 
 
+def gather_ceiling(dtype, num_cols: int, num_gathers: int, stream=None) -> tuple[float, float]:
+    """Measured random-gather rate (gathers/s) from a vector of num_cols
+    values, the bound of SpMV on matrices with random column indices, and the
+    kernel's checksum (sum of its per-thread sums)."""
+    rate, chk = C.c_double(0.0), C.c_double(0.0)
+    call("sspmv_gather_ceiling", _vt(dtype), int(num_cols), int(num_gathers), C.byref(rate), C.byref(chk),
+         _stream(stream))
+    return rate.value, chk.value
+
+
 def read_csr_matrix(path: str, precision: int = 64) -> HostCSR:
     """read_csr_matrix (utils/sparse_io.cpp:180-204) on the host."""
     vt = F64 if precision == 64 else F32

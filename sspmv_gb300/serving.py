@@ -322,6 +322,10 @@ def select_formats(mats: list[dict], model_path, min_nnz: int = 1_000_000, log=N
     return out
 
 
+def _us(v) -> str:
+    return "n/a" if v is None else f"{v:.0f} us"
+
+
 def serving_benchmark(num_matrices: int = 64, device_buffers: bool = False, duration_s: float = 1.5,
                       seed: int = 0, log=None, selector_model=None) -> dict:
     """Saturation throughput of the batched server and of per-request CSR
@@ -376,8 +380,8 @@ def serving_benchmark(num_matrices: int = 64, device_buffers: bool = False, dura
                 r = b.run(m["_server"], n, rate, seed + 10 + int(f * 100))
                 r["fraction_of_per_request_saturation"] = f
                 m["sweep"].append(r)
-                log(f"[serving] {mode} @ {rate:.0f}/s: {r['req_per_s']:.0f} req/s p50 {r['p50_us']:.0f} us "
-                    f"p99 {r['p99_us']:.0f} us batch {r['mean_batch']:.1f}")
+                log(f"[serving] {mode} @ {rate:.0f}/s: {r['req_per_s']:.0f} req/s p50 {_us(r['p50_us'])} "
+                    f"p99 {_us(r['p99_us'])} batch {r['mean_batch']:.1f} failed {r['failed']}")
             m["stats"] = m["_server"].stats()
     finally:
         for mode in res["modes"].values():

@@ -229,3 +229,26 @@ def test_deterministic_bits(fmt):
         L.LeSpMV(1.0, G, x, 0.0, y)
         outs.append(to_host(y))
     assert all(np.array_equal(outs[0], o) for o in outs[1:])
+
+
+@pytest.mark.parametrize("fmt", ["sell_c4", "scs_c8", "scr_c16", "sell"])
+def test_sliced_overflow_caps(fmt, oracle_lib):
+    """Thread-pass caps set through sspmv_set_kernel's param (0 = cost model):
+    rows longer than the cap finish in the overflow CSR pass; results stay
+    within tolerance at every cap and after the cap changes."""
+    from sspmv_gb300 import lespmv as L
+    from sspmv_gb300 import synth
+    A = synth.generate(FAMILIES["powerlaw"](synth), 3, np.float64)
+    M = L.csr_from_host(A)
+    G = GPU_CONV[fmt](L, M)
+    nnz_row = np.diff(A.row_offset)
+    for cap in (1, 4, 8, 33, 0, 1 << 30, 16):
+        G.set_kernel(0, cap)
+        for k in (1, 3, 8):
+            X = synth.vector(A.num_cols, 0, np.float64, k).reshape(A.num_cols, k)
+            Y0 = synth.vector(A.num_rows, 9, np.float64, k).reshape(A.num_rows, k)
+            Y = to_dev(Y0)
+            L.spmm(ALPHA, G, to_dev(X), BETA, Y)
+            y64, absum = oracle_lib.spmm_ref(A, X, ALPHA, BETA, Y0)
+            ok, mx, _ = tolerance_ok(to_host(Y), y64, absum, nnz_row, np.float64, ALPHA, BETA, Y0)
+            assert ok, f"{fmt}/cap={cap}/k={k}: max normalised error {mx}"

@@ -122,6 +122,38 @@ def test_batched_csr_equals_single_request_entry_point():
         assert np.array_equal(to_host(Y), y), f"matrix {mid} k={k}: batched differs from sspmv_spmm_csr"
 
 
+def _long_row_matrix(seed, m=600, long_len=3000):
+    """A small CSR matrix whose row 7 spans more than ten 256-nonzero chunks
+    (its other rows 1..12 nonzeros), so rows crossing many chunks of different
+    matrices meet in one warp of the batched fix-up."""
+    from sspmv_gb300 import synth
+    rng = np.random.default_rng(seed)
+    lens = rng.integers(1, 13, m)
+    lens[7] = long_len
+    rp = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    cols = np.concatenate([np.sort(rng.choice(8000, size=l, replace=False)) for l in lens]).astype(np.int32)
+    vals = rng.uniform(-1, 1, rp[-1])
+    return synth.HostCSR(m, 8000, rp, cols, vals)
+
+
+def test_batched_long_rows_across_many_small_matrices(oracle_lib):
+    """Dozens of small matrices in one batch, each with a row spanning many
+    chunks: equal to the single-request entry point bit for bit."""
+    from sspmv_gb300.lespmv import csr_from_host, spmm
+    mats = {m: (_long_row_matrix(m, long_len=1500 + 97 * m), "csr", None) for m in range(40)}
+    reqs = [(m, 1 + (m % 2), BETA if m % 3 else 0.0) for m in mats]
+    xs, y0s = _buffers(mats, reqs, seed=70)
+    with _server(mats) as s:
+        ys, infos = _mixed(s, reqs, xs, y0s)
+    assert infos["batch_size"].max() > 1
+    dev = {m: csr_from_host(v[0]) for m, v in mats.items()}
+    for (mid, k, beta), x, y0, y in zip(reqs, xs, y0s, ys):
+        Y = to_dev(y0)
+        spmm(ALPHA, dev[mid], to_dev(x), beta, Y)
+        assert np.array_equal(to_host(Y), y), f"matrix {mid} k={k}: batched differs from sspmv_spmm_csr"
+    _check_oracle(oracle_lib, mats, reqs, xs, y0s, ys)
+
+
 @pytest.mark.parametrize("graphs", [True, False], ids=["graphs", "direct"])
 def test_per_request_mode_and_direct_launches_match(graphs):
     mats = _matrices()
