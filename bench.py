@@ -210,6 +210,8 @@ def run_gpu(args, rank, world):
                     c["M"] = M2
                     c["bytes"] = M2.algorithmic_bytes(1, False)
                     c["tuned"] = {"params": rec["params"], "ms": rec["ms"]}
+                    if rec.get("kernel"):
+                        c["tuned"]["kernel"] = {k: rec["kernel"][k] for k in ("kernel_flag", "param")}
                 log(f"tuned {c['fam']}/{c['fmt']}/{c['dt']}: {c.get('tuned')}")
                 continue
             res = autotune.tune_format(c["M"], c["x"], c["y"])

@@ -7,6 +7,8 @@ fastest is kept.  Results are plain dicts, so a caller can store them as an
 append-only JSONL log keyed by matrix and re-apply them without re-measuring.
 
 CSR candidates: stream kernel (default), merge-path kernel, vector kernel with 2..32 lanes per row.
+S-ELL / SELL-c-sigma / SELL-c-R: after the layout, the thread-pass cap (the
+cost model's choice against caps of 16..128 slots).
 SELL-c-sigma candidates (re-conversion per point): C in {8,16,32} x sigma in
 {256, 4096, N}.  BSR candidates: r x c in {2,4,8,16}^2 (feasible ones).
 """
@@ -60,8 +62,12 @@ def tune_csr(M, x, y, reps: int = 10) -> dict:
     return tune_kernel(M, x, y, CSR_CANDIDATES, reps)
 
 
+# Sliced formats: the thread-pass cap (param; 0 = the library's cost model).
+SLICED_CAPS = [(0, 0), (0, 16), (0, 32), (0, 64), (0, 128)]
+
 # Kernel candidates per format (formats with one kernel are not listed).
-KERNEL_CANDIDATES = {"csr": CSR_CANDIDATES, "coo": [(0, 0), (1, 0)]}
+KERNEL_CANDIDATES = {"csr": CSR_CANDIDATES, "coo": [(0, 0), (1, 0)], "sell": SLICED_CAPS,
+                     "sell_c_sigma": SLICED_CAPS, "sell_c_R": SLICED_CAPS}
 
 
 def conversion_candidates(fmt: str, num_rows: int) -> list[dict]:

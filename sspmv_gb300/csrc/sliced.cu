@@ -105,11 +105,11 @@ __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
     }
 }
 
-// Long tails (kPieceMin nonzeros or more) are cut into pieces of at most
-// kPieceElems nonzeros of one row, a warp per piece, lanes on consecutive
-// elements; piece = {overflow row, first element, end element} of the
-// compact arrays.
-constexpr int64_t kPieceMin = 1024;
+// Long tails (kPieceMin nonzeros or more; 64 measured best against 256, 1024
+// and 4096) are cut into pieces of at most kPieceElems nonzeros of one row, a
+// warp per piece, lanes on consecutive elements; piece = {overflow row, first
+// element, end element} of the compact arrays.
+constexpr int64_t kPieceMin = 64;
 constexpr int64_t kPieceElems = 2048;
 
 template <typename V, int K>

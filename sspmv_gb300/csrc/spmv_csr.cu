@@ -714,20 +714,22 @@ __device__ __forceinline__ void stream_chunk_lanes(
     }
 }
 
-// The chunk of a matrix without empty rows whose nonzeros lie in at most
-// kFastRows + 1 rows (a warp-uniform test): lane j reads rp[ra + j] once, and
-// each lane finds the row of its first nonzero and the ends of the next
-// eight rows by shuffles -- no chain of dependent loads on row_offset.  The
-// arithmetic (per-lane sums in nonzero order, the segmented scan, the carry
-// slots) is that of stream_chunk_lanes, so both give the same bits.
-constexpr int kFastRows = 32 - kStreamPerLane - 1;
-
+// The chunk of a matrix without empty rows: the rows starting inside the
+// chunk are read once (row_offset[ra ..], one row per lane per step) and
+// marked as bits in shared memory (one 8-bit word per lane, position p of the
+// chunk at word p / 8, bit p % 8); each lane then knows which of its 8
+// nonzeros end a row (the next position starts one) and, by a prefix count of
+// the bits, the row of its first nonzero -- no search and no chain of
+// dependent loads on row_offset.  The arithmetic (per-lane sums in nonzero
+// order, the segmented scan, the carry slots) is that of stream_chunk_lanes,
+// so both give the same bits.  sbits: the warp's 33 words of shared memory.
 template <typename V, int K>
 __device__ __forceinline__ void stream_chunk_fast(
     int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy, const int ra,
-    const int64_t w, const int64_t slot, int32_t *__restrict__ carry_row, int32_t *__restrict__ has_end,
-    V *__restrict__ carry_val, V *__restrict__ head_val, int vec) {
+    const int last, const int64_t w, const int64_t slot, int32_t *__restrict__ carry_row,
+    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val, int vec,
+    uint32_t *__restrict__ sbits) {
     constexpr unsigned kFull = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int64_t j0 = w * kStreamChunk;
@@ -737,25 +739,34 @@ __device__ __forceinline__ void stream_chunk_fast(
     int c[8];
     V a[8];
     stream_load8<V>(ci, cv, e0, nv, vec != 0, c, a);
-    // R_j = rp[ra + j]: the starts of rows ra .. ra + 31 (past the end: never <= e0)
-    const int rl = ra + lane <= m ? __ldg(rp + ra + lane) : 0x7fffffff;
-    const bool head_open = __shfl_sync(kFull, rl, 0) < j0;  // the chunk's first row began in an earlier chunk
-    // largest p with R_p <= e0 (R_0 <= j0 <= e0): the lane's first row is ra + p
-    int pos = 0;
-#pragma unroll
-    for (int step = 16; step >= 1; step >>= 1) {
-        const int v = __shfl_sync(kFull, rl, (pos + step) & 31);
-        if (pos + step <= 31 && (int64_t)v <= e0) pos += step;
+    sbits[lane] = 0u;
+    if (lane == 0) sbits[32] = 0u;
+    __syncwarp();
+    // rows ra .. last (last = one past the row holding the chunk's end): mark
+    // each start p in (0, 256] (p = 256: a row starting right after the chunk)
+    bool head_open = false;
+    for (int r0 = ra; r0 <= last; r0 += 32) {  // warp-uniform
+        const int rr = r0 + lane;
+        if (rr <= last) {
+            const int64_t p = (int64_t)__ldg(rp + rr) - j0;
+            if (p > 0 && p <= kStreamChunk) atomicOr(sbits + (p >> 3), 1u << (p & 7));
+            if (rr == ra) head_open = p < 0;  // the chunk's first row began in an earlier chunk
+        }
     }
-    // bit u of `ends`: the lane's nonzero u is the last of its row (row ends
-    // R_{pos+1} .. R_{pos+8} that fall on e0+1 .. e0+8)
-    uint32_t ends = 0;
+    head_open = __shfl_sync(kFull, head_open, 0);
+    __syncwarp();
+    const uint32_t starts = sbits[lane], starts_next = sbits[lane + 1];
+    // bit u of `ends`: nonzero u ends its row (a row starts at e0 + u + 1)
+    const uint32_t ends = (starts >> 1) | ((starts_next & 1u) << 7);
+    // the lane's first row: ra + the starts in (j0, e0]
+    int before = __popc(starts);
 #pragma unroll
-    for (int k = 1; k <= kStreamPerLane; k++) {
-        const int v = __shfl_sync(kFull, rl, (pos + k) & 31);
-        const int64_t u = (int64_t)v - 1 - e0;
-        if (pos + k <= 31 && u >= 0 && u < kStreamPerLane) ends |= 1u << u;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(kFull, before, o);
+        if (lane >= o) before += t;
     }
+    before -= __popc(starts);  // starts in lanes before this one
+    const int pos = before + (int)(starts & 1u);
     V xv[K <= 2 ? 8 : 1][K];
     if constexpr (K <= 2) {
 #pragma unroll
@@ -855,23 +866,29 @@ __device__ __forceinline__ void stream_chunk(
     int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
     const int32_t *__restrict__ row_start, const int64_t w, const int64_t slot, int32_t *__restrict__ carry_row,
-    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val, int vec, int no_empty) {
+    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val, int vec, int no_empty,
+    uint32_t *__restrict__ sbits) {
     if constexpr (K == 8 && sizeof(V) == 8) {
         stream_chunk_cols<V, K, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, slot, carry_row,
                                    has_end, carry_val, head_val);
     } else {
         if (no_empty && w * kStreamChunk < nnz) {  // warp-uniform
             const int ra = __ldg(row_start + w);
-            if (min(__ldg(row_start + w + 1), m - 1) - ra <= kFastRows) {
-                stream_chunk_fast<V, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, ra, w, slot, carry_row,
-                                        has_end, carry_val, head_val, vec);
-                return;
-            }
+            const int last = min(__ldg(row_start + w + 1), m - 1) + 1;
+            stream_chunk_fast<V, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, ra, last, w, slot, carry_row,
+                                    has_end, carry_val, head_val, vec, sbits);
+            return;
         }
         stream_chunk_lanes<V, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, slot, carry_row,
                                  has_end, carry_val, head_val, vec);
     }
 }
+
+#define SSPMV_STREAM_KERNEL_BODY                                                                          \
+    __shared__ uint32_t s_bits[kBlock / 32][33];                                                          \
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;                              \
+    stream_chunk<V, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, w, carry_row, has_end, \
+                       carry_val, head_val, vec, no_empty, s_bits[threadIdx.x >> 5]);
 
 template <typename V, int K>
 __global__ void __launch_bounds__(kBlock) csr_stream_kernel(
@@ -879,10 +896,20 @@ __global__ void __launch_bounds__(kBlock) csr_stream_kernel(
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
     const int32_t *__restrict__ row_start, int32_t *__restrict__ carry_row, int32_t *__restrict__ has_end,
     V *__restrict__ carry_val, V *__restrict__ head_val, int vec, int no_empty) {
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    stream_chunk<V, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, w, carry_row, has_end,
-                       carry_val, head_val, vec, no_empty);
+    SSPMV_STREAM_KERNEL_BODY
 }
+
+// The same kernel held to six resident CTAs per SM (at most 42 registers):
+// measured 5-8% faster for FP32 at k = 1; FP64 slows down when squeezed.
+template <typename V, int K>
+__global__ void __launch_bounds__(kBlock, 6) csr_stream_kernel_occ6(
+    int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
+    const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
+    const int32_t *__restrict__ row_start, int32_t *__restrict__ carry_row, int32_t *__restrict__ has_end,
+    V *__restrict__ carry_val, V *__restrict__ head_val, int vec, int no_empty) {
+    SSPMV_STREAM_KERNEL_BODY
+}
+#undef SSPMV_STREAM_KERNEL_BODY
 
 // Rows crossing chunks: a thread per chunk; the chunk where the row starts
 // adds the later chunks' pieces (chain_sum).
@@ -949,10 +976,18 @@ sspmv_status launch_stream(const sspmv_csr *A, Plan *p, V alpha, const V *x, int
     const int64_t nt = p->extra_i[0];
     int32_t *ints = (int32_t *)p->extra[1];
     const int vec = ((reinterpret_cast<uintptr_t>(A->col_index) | reinterpret_cast<uintptr_t>(A->values)) & 15) == 0;
-    csr_stream_kernel<V, K><<<grid_for(nt * 32, kBlock), kBlock, 0, cu(s)>>>(
-        (int)A->f.num_rows, A->f.num_nnzs, A->row_offset, A->col_index, (const V *)A->values, x, ldx, alpha, beta,
-        y, ldy, (const int32_t *)p->extra[0], ints, ints + nt, (V *)p->extra[2], (V *)p->extra[3], vec,
-        p->extra_i[1] == 0 ? 1 : 0);
+    const unsigned grid = grid_for(nt * 32, kBlock);
+    const int no_empty = p->extra_i[1] == 0 ? 1 : 0;
+    if constexpr (sizeof(V) == 4 && K == 1)
+        csr_stream_kernel_occ6<V, K><<<grid, kBlock, 0, cu(s)>>>(
+            (int)A->f.num_rows, A->f.num_nnzs, A->row_offset, A->col_index, (const V *)A->values, x, ldx, alpha,
+            beta, y, ldy, (const int32_t *)p->extra[0], ints, ints + nt, (V *)p->extra[2], (V *)p->extra[3], vec,
+            no_empty);
+    else
+        csr_stream_kernel<V, K><<<grid, kBlock, 0, cu(s)>>>(
+            (int)A->f.num_rows, A->f.num_nnzs, A->row_offset, A->col_index, (const V *)A->values, x, ldx, alpha,
+            beta, y, ldy, (const int32_t *)p->extra[0], ints, ints + nt, (V *)p->extra[2], (V *)p->extra[3], vec,
+            no_empty);
     SSPMV_LAUNCH_CHECK();
     if (nt > 1) {
         csr_stream_fixup<V, K><<<grid_for(nt, 256), 256, 0, cu(s)>>>(nt, A->row_offset, ints, ints + nt,
@@ -996,7 +1031,7 @@ __global__ void __launch_bounds__(kBlock) csr_batch_kernel(int g, const BatchHea
         const BatchItem *q = items + batch_item_of(items, n, gc);
         stream_chunk<V, K>(q->m, q->nnz, q->row_offset, q->col_index, (const V *)q->values, (const V *)q->x, q->ldx,
                            (V)q->alpha, (V)q->beta, (V *)q->y, q->ldy, q->row_start, gc - q->chunk_begin, base + gc,
-                           carry_row, has_end, carry_val, head_val, q->vec, 0);
+                           carry_row, has_end, carry_val, head_val, q->vec, 0, nullptr);
     }
 }
 
