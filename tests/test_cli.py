@@ -63,3 +63,22 @@ def test_cli_runs_and_appends_reference_line(tmp_path, fmt, precision):
     assert "Performing 30 iterations" in r.stdout
     line = (tmp_path / "performance" / "mat_perf.txt").read_text().splitlines()[-1] + "\n"
     assert re.match(LINES[fmt], line.rstrip("\n")), repr(line)
+
+
+def test_profile_case_usage():
+    """The one-case profiling driver parses its arguments without a GPU."""
+    import sys
+    r = subprocess.run([sys.executable, "-m", "sspmv_gb300.profile_case", "--help"], capture_output=True, text=True)
+    assert r.returncode == 0 and "family" in r.stdout
+    r = subprocess.run([sys.executable, "-m", "sspmv_gb300.profile_case", "powerlaw_4M", "nosuchformat", "f64"],
+                       capture_output=True, text=True)
+    assert r.returncode != 0
+
+
+@pytest.mark.gpu
+def test_profile_case_runs():
+    import sys
+    r = subprocess.run([sys.executable, "-m", "sspmv_gb300.profile_case", "banded_2M", "csr", "f32", "--reps", "1"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    assert "banded_2M csr f32 ms" in r.stdout
