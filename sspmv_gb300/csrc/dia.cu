@@ -91,8 +91,10 @@ __global__ void __launch_bounds__(kBlock) dia_spmv_kernel(int m, int n, int nd, 
             V a[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
+                // data[d][i] exists for every row i < m (stride >= m): the load
+                // does not wait for the offset that decides whether it is used
                 j[u] = i + __ldg(offsets + d + u);
-                a[u] = (j[u] >= 0 && j[u] < n) ? ld_stream(data + (int64_t)(d + u) * stride + i) : V(0);
+                a[u] = ld_stream(data + (int64_t)(d + u) * stride + i);
             }
 #pragma unroll
             for (int u = 0; u < 4; u++)

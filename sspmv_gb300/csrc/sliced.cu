@@ -49,6 +49,8 @@ constexpr int kBlock = 256;
 // row, a warp each; a fix-up adds each overflow row's thread partial and the
 // rest.  The compact copy also skips the padding of the short rows that
 // share a long row's chunk (slot-major storage puts them in the same sectors).
+constexpr int kSlots = 4;  // slots of a row whose loads are in flight together
+
 template <typename V, int K>
 __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
     int m, int C, const int64_t *__restrict__ chunk_ptr, const int32_t *__restrict__ reorder,
@@ -67,23 +69,23 @@ __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
 #pragma unroll
         for (int q = 0; q < K; q++) s[q] = V(0);
         int64_t k = 0;
-        for (; k + 4 <= w; k += 4) {
-            int cc[4];
-            V aa[4];
+        for (; k + kSlots <= w; k += kSlots) {
+            int cc[kSlots];
+            V aa[kSlots];
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
+            for (int u = 0; u < kSlots; u++) {
                 cc[u] = ld_stream(cp + (k + u) * C);
                 aa[u] = ld_stream(vp + (k + u) * C);
             }
 #pragma unroll
-            for (int u = 0; u < 4; u++)
+            for (int u = 0; u < kSlots; u++)
                 if (cc[u] >= 0) {
 #pragma unroll
                     for (int q = 0; q < K; q++) s[q] += aa[u] * ld_x(x + (int64_t)cc[u] * ldx + q);
                 }
-            if (cc[3] < 0) break;  // padding is a suffix of the row
+            if (cc[kSlots - 1] < 0) break;  // padding is a suffix of the row
         }
-        if (k + 4 > w) {
+        if (k + kSlots > w) {
             for (; k < w; k++) {
                 const int cc = ld_stream(cp + k * C);
                 if (cc < 0) break;
