@@ -38,10 +38,49 @@ __global__ void fill_i32(int64_t n, int32_t v, int32_t *__restrict__ p) {
         p[i] = v;
 }
 
+// first[d] = smallest CSR position on diagonal d (the reference's
+// first-encounter order).  Where the 32 rows of a warp start on a few common
+// diagonals (banded matrices), the warp walks them in step (k-th nonzero of
+// each row together), groups the lanes on the same diagonal and lets only the
+// lowest one -- the smallest row, so the smallest position -- issue the
+// atomicMin: one atomic per diagonal per warp instead of one per nonzero to
+// the same few addresses.  Other warps (scattered diagonals, where lockstep
+// would only add work) walk their rows one thread per row.
 __global__ void dia_first_pos(int64_t m, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
                               int32_t *__restrict__ first) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
-        for (int32_t jj = rp[i]; jj < rp[i + 1]; jj++) atomicMin(&first[m - i + ci[jj]], jj);
+    constexpr unsigned kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane; base < m;
+         base += (int64_t)gridDim.x * blockDim.x) {  // warp-uniform
+        const int64_t i = base + lane;
+        int32_t j0 = 0, len = 0;
+        if (i < m) {
+            j0 = rp[i];
+            len = rp[i + 1] - j0;
+        }
+        const bool act0 = len > 0;
+        const unsigned on0 = __ballot_sync(kFull, act0);
+        bool leader0 = false;
+        if (act0) {
+            const unsigned grp = __match_any_sync(on0, (unsigned long long)(m - i + ci[j0]));
+            leader0 = lane == __ffs(grp) - 1;
+        }
+        if (__popc(__ballot_sync(kFull, leader0)) > 4) {  // scattered: a thread per row
+            for (int32_t jj = j0; jj < j0 + len; jj++) atomicMin(&first[m - i + ci[jj]], jj);
+            continue;
+        }
+        const int32_t most = __reduce_max_sync(kFull, (unsigned)len);
+        for (int32_t k = 0; k < most; k++) {
+            const bool act = k < len;
+            const unsigned on = __ballot_sync(kFull, act);
+            if (act) {
+                const int32_t jj = j0 + k;
+                const unsigned long long key = (unsigned long long)(m - i + ci[jj]);
+                const unsigned grp = __match_any_sync(on, key);
+                if (lane == __ffs(grp) - 1) atomicMin(&first[key], jj);
+            }
+        }
+    }
 }
 
 __global__ void dia_collect(int64_t len, const int32_t *__restrict__ first, int32_t cap,

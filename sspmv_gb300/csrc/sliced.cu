@@ -546,21 +546,49 @@ __global__ void chunk_widths(int64_t nchunks, int32_t C, int32_t align, int32_t 
     }
 }
 
+// Copies the CSR rows into the slab: a thread per stored row, except rows of
+// kFillLong nonzeros or more, which the CTA holding them copies together
+// after its short rows (one thread walking a 38k-nonzero row alone took
+// milliseconds).
+constexpr int64_t kFillLong = 256;
+
 template <typename V>
-__global__ void sliced_fill(int64_t m, int32_t C, const int64_t *__restrict__ chunk_ptr,
-                            const int32_t *__restrict__ reorder, const int32_t *__restrict__ rp,
-                            const int32_t *__restrict__ ci, const V *__restrict__ cv, int32_t *__restrict__ col,
-                            V *__restrict__ val) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t c = i / C;
-        const int64_t q = i - c * C;
-        const int64_t r = reorder ? reorder[i] : i;
-        const int64_t s0 = rp[r], len = rp[r + 1] - s0;
-        const int64_t base = chunk_ptr[c] + q;
-        for (int64_t k = 0; k < len; k++) {
-            col[base + k * C] = ci[s0 + k];
-            val[base + k * C] = cv[s0 + k];
+__global__ void __launch_bounds__(256) sliced_fill(int64_t m, int32_t C, const int64_t *__restrict__ chunk_ptr,
+                                                   const int32_t *__restrict__ reorder,
+                                                   const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
+                                                   const V *__restrict__ cv, int32_t *__restrict__ col,
+                                                   V *__restrict__ val) {
+    __shared__ int64_t s_long[256];
+    __shared__ int s_count;
+    for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x; b0 < m; b0 += (int64_t)gridDim.x * blockDim.x) {
+        if (threadIdx.x == 0) s_count = 0;
+        __syncthreads();
+        const int64_t i = b0 + threadIdx.x;
+        if (i < m) {
+            const int64_t r = reorder ? reorder[i] : i;
+            const int64_t s0 = rp[r], len = rp[r + 1] - s0;
+            if (len >= kFillLong) {
+                s_long[atomicAdd(&s_count, 1)] = i;
+            } else {
+                const int64_t base = chunk_ptr[i / C] + i % C;
+                for (int64_t k = 0; k < len; k++) {
+                    col[base + k * C] = ci[s0 + k];
+                    val[base + k * C] = cv[s0 + k];
+                }
+            }
         }
+        __syncthreads();
+        for (int t = 0; t < s_count; t++) {  // CTA-uniform
+            const int64_t li = s_long[t];
+            const int64_t r = reorder ? reorder[li] : li;
+            const int64_t s0 = rp[r], len = rp[r + 1] - s0;
+            const int64_t base = chunk_ptr[li / C] + li % C;
+            for (int64_t k = threadIdx.x; k < len; k += blockDim.x) {
+                col[base + k * C] = ci[s0 + k];
+                val[base + k * C] = cv[s0 + k];
+            }
+        }
+        __syncthreads();  // s_long / s_count are reused by the next round
     }
 }
 

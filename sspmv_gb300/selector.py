@@ -488,6 +488,26 @@ def common_params(paths) -> dict:
     return {f: json.loads(c.most_common(1)[0][0]) for f, c in cnt.items() if c}
 
 
+def pack_dataset(paths, out) -> None:
+    """Writes labelled JSONL records as one .npz: raw features, times per
+    format (inf: infeasible), matrix ids, family, rows, nonzeros and the most
+    frequent best parameters per format (JSON bytes) -- the layout of
+    sspmv_gb300/data/selector_dataset.npz."""
+    ds = load_dataset(paths)
+    recs = {}
+    for p in ([paths] if isinstance(paths, (str, Path)) else paths):
+        for ln in Path(p).read_text().splitlines():
+            if ln.strip():
+                r = json.loads(ln)
+                recs[r["i"]] = r
+    fam = np.array([recs[int(i)]["family"] for i in ds.ids])
+    rows = np.array([recs[int(i)]["num_rows"] for i in ds.ids], np.int64)
+    nnz = np.array([recs[int(i)]["nnz"] for i in ds.ids], np.int64)
+    params = np.frombuffer(json.dumps(common_params(paths)).encode(), np.uint8)
+    np.savez(out, raw=ds.raw, times=ds.times, ids=ds.ids, family=fam, num_rows=rows, nnz=nnz,
+             format_params=params)
+
+
 class Selector:
     """A trained network and the parameter set it uses per format; picks the
     serving format of a device CSR matrix."""
@@ -505,6 +525,7 @@ class Selector:
 
 def main(argv=None) -> None:
     """python -m sspmv_gb300.selector dataset --out FILE --count N [--start S]
+       python -m sspmv_gb300.selector pack --data FILE [FILE...] --out DATASET.npz
        python -m sspmv_gb300.selector train --data FILE [FILE...] --model OUT.npz --report OUT.json"""
     import argparse
     import sys
@@ -516,6 +537,9 @@ def main(argv=None) -> None:
     d.add_argument("--start", type=int, default=0)
     d.add_argument("--seed", type=int, default=0)
     d.add_argument("--budget-s", type=float, default=0.0, help="stop after this many seconds (0: no limit)")
+    pk = sub.add_parser("pack", help="JSONL label files -> one .npz (the packaged dataset layout)")
+    pk.add_argument("--data", nargs="+", required=True)
+    pk.add_argument("--out", required=True)
     t = sub.add_parser("train")
     t.add_argument("--data", nargs="+", required=True)
     t.add_argument("--model", required=True)
@@ -532,6 +556,9 @@ def main(argv=None) -> None:
                 log(f"[dataset] budget reached before matrix {s}")
                 break
             build_dataset(a.out, min(step, a.start + a.count - s), s, a.seed, log)
+        return
+    if a.cmd == "pack":
+        pack_dataset(a.data, a.out)
         return
     ds = load_dataset(a.data[0] if len(a.data) == 1 and a.data[0].endswith(".npz") else a.data)
     net, res = evaluate(ds, 0.8, a.seed, a.epochs, log)
