@@ -231,24 +231,55 @@ def test_deterministic_bits(fmt):
     assert all(np.array_equal(outs[0], o) for o in outs[1:])
 
 
+@pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
 @pytest.mark.parametrize("fmt", ["sell_c4", "scs_c8", "scr_c16", "sell"])
-def test_sliced_overflow_caps(fmt, oracle_lib):
+def test_sliced_overflow_caps(fmt, dt, oracle_lib):
     """Thread-pass caps set through sspmv_set_kernel's param (0 = cost model):
     rows longer than the cap finish in the overflow CSR pass; results stay
     within tolerance at every cap and after the cap changes."""
     from sspmv_gb300 import lespmv as L
     from sspmv_gb300 import synth
-    A = synth.generate(FAMILIES["powerlaw"](synth), 3, np.float64)
+    A = synth.generate(FAMILIES["powerlaw"](synth), 3, dt)
     M = L.csr_from_host(A)
     G = GPU_CONV[fmt](L, M)
     nnz_row = np.diff(A.row_offset)
     for cap in (1, 4, 8, 33, 0, 1 << 30, 16):
         G.set_kernel(0, cap)
         for k in (1, 3, 8):
-            X = synth.vector(A.num_cols, 0, np.float64, k).reshape(A.num_cols, k)
-            Y0 = synth.vector(A.num_rows, 9, np.float64, k).reshape(A.num_rows, k)
+            X = synth.vector(A.num_cols, 0, dt, k).reshape(A.num_cols, k)
+            Y0 = synth.vector(A.num_rows, 9, dt, k).reshape(A.num_rows, k)
             Y = to_dev(Y0)
             L.spmm(ALPHA, G, to_dev(X), BETA, Y)
             y64, absum = oracle_lib.spmm_ref(A, X, ALPHA, BETA, Y0)
-            ok, mx, _ = tolerance_ok(to_host(Y), y64, absum, nnz_row, np.float64, ALPHA, BETA, Y0)
+            ok, mx, _ = tolerance_ok(to_host(Y), y64, absum, nnz_row, dt, ALPHA, BETA, Y0)
             assert ok, f"{fmt}/cap={cap}/k={k}: max normalised error {mx}"
+
+
+def test_dia_converter_mixed_warps(oracle_lib):
+    """A banded matrix with scattered extra entries in some rows: warps whose
+    rows share diagonals (grouped atomics) and warps that do not (one thread
+    per row) in one conversion; arrays bit-exact against the oracle."""
+    from sspmv_gb300 import lespmv as L
+    from sspmv_gb300 import synth
+    rng = np.random.default_rng(11)
+    m = 20000
+    rows, cols = [], []
+    for i in range(m):
+        cs = {j for j in (i - 3, i - 1, i, i + 1, i + 3) if 0 <= j < m}
+        if (i // 64) % 5 == 0:  # scattered entries on 40 far diagonals, after the band
+            cs |= {j for j in (i + 500 + int(rng.integers(0, 40)),) if j < m}
+        if (i // 32) % 7 == 3:  # whole warps whose rows start on different diagonals
+            cs |= {j for j in (i - 700 - int(rng.integers(0, 40)),) if j >= 0}
+        rows += [i] * len(cs)
+        cols += sorted(cs)
+    rows, cols = np.array(rows), np.array(cols, np.int32)
+    rp = np.zeros(m + 1, np.int32)
+    np.add.at(rp, rows + 1, 1)
+    rp = np.cumsum(rp).astype(np.int32)
+    A = synth.HostCSR(m, m, rp, cols, rng.uniform(-1, 1, len(cols)))
+    ref = oracle_lib.csr_to_dia(A)
+    assert ref is not None
+    out = L.csr_to_dia(L.csr_from_host(A)).export()
+    for name, arr in ref.items():
+        if isinstance(arr, np.ndarray):
+            assert np.array_equal(out[name].view(np.uint8), arr.view(np.uint8)), name
