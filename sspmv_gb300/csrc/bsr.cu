@@ -97,8 +97,8 @@ template <typename V, int K, int CB>
 __global__ void __launch_bounds__(kBlock) bsr_spmv_kernel(int m, int n, int r, int cr,
                                                         const int32_t *__restrict__ row_ptr,
                                                         const int32_t *__restrict__ bcol, const V *__restrict__ data,
-                                                        const V *__restrict__ x, int64_t ldx, V alpha, V beta,
-                                                        V *__restrict__ y, int64_t ldy) {
+                                                        const V *__restrict__ x, int64_t ldx, int xvec, V alpha,
+                                                        V beta, V *__restrict__ y, int64_t ldy) {
     const int c = CB > 0 ? CB : cr;
     const int64_t rc = (int64_t)r * c;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
@@ -115,15 +115,20 @@ __global__ void __launch_bounds__(kBlock) bsr_spmv_kernel(int m, int n, int r, i
 #pragma unroll
                 for (int e = 0; e < (CB > 0 ? CB : 1); e++) a[e] = ld_stream(blk + e);
 #pragma unroll
-                for (int e = 0; e < (CB > 0 ? CB : 1); e++)
+                for (int e = 0; e < (CB > 0 ? CB : 1); e++) {
+                    V xr[K];
+                    ld_xrow<V, K>(x, x0 + e, ldx, xvec != 0, xr);
 #pragma unroll
-                    for (int t = 0; t < K; t++) s[t] += a[e] * ld_x(x + (x0 + e) * ldx + t);
+                    for (int t = 0; t < K; t++) s[t] += a[e] * xr[t];
+                }
             } else {
                 for (int e = 0; e < c; e++) {
                     if (x0 + e >= n) break;
                     const V a = ld_stream(blk + e);
+                    V xr[K];
+                    ld_xrow<V, K>(x, x0 + e, ldx, xvec != 0, xr);
 #pragma unroll
-                    for (int t = 0; t < K; t++) s[t] += a * ld_x(x + (x0 + e) * ldx + t);
+                    for (int t = 0; t < K; t++) s[t] += a * xr[t];
                 }
             }
         }
@@ -139,7 +144,8 @@ sspmv_status launch_bsr_c(const sspmv_bsr *A, V alpha, const V *x, int64_t ldx, 
     const unsigned grid = grid_for(A->f.num_rows, kBlock, (int64_t)num_sms() * 16);
     bsr_spmv_kernel<V, K, CB><<<grid, kBlock, 0, cu(s)>>>((int)A->f.num_rows, (int)A->f.num_cols, (int)A->blockDim_r,
                                                           (int)A->blockDim_c, A->row_ptr, A->block_colindex,
-                                                          (const V *)A->block_data, x, ldx, alpha, beta, y, ldy);
+                                                          (const V *)A->block_data, x, ldx,
+                                                          xrow_vec(x, ldx, sizeof(V), K), alpha, beta, y, ldy);
     SSPMV_LAUNCH_CHECK();
     return SSPMV_OK;
 }

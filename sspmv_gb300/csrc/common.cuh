@@ -106,6 +106,52 @@ __device__ __forceinline__ T ld_stream(const T *p) { return __ldcs(p); }
 template <typename T>
 __device__ __forceinline__ T ld_x(const T *p) { return __ldg(p); }
 
+// Row j of a row-major block X of K right-hand sides (leading dimension ldx
+// values): with `vec` set, one vector load per 16 bytes of the row (8 bytes
+// for FP32 with K = 2), else K scalar loads; read-only cached like ld_x.  A
+// warp gathering K-wide rows this way touches each row's sector once instead
+// of once per column (K scalar loads are K separate L1 lookups per lane).
+template <typename V, int K>
+__device__ __forceinline__ void ld_xrow(const V *__restrict__ x, int64_t j, int64_t ldx, bool vec, V (&out)[K]) {
+    const V *p = x + j * ldx;
+    if constexpr (K >= 2 && K * sizeof(V) >= 8) {
+        if (vec) {
+            if constexpr (sizeof(V) == 8) {
+#pragma unroll
+                for (int h = 0; h < K / 2; h++) {
+                    const double2 v = __ldg(reinterpret_cast<const double2 *>(p) + h);
+                    out[2 * h] = v.x;
+                    out[2 * h + 1] = v.y;
+                }
+            } else if constexpr (K == 2) {
+                const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+                out[0] = v.x;
+                out[1] = v.y;
+            } else {
+#pragma unroll
+                for (int h = 0; h < K / 4; h++) {
+                    const float4 v = __ldg(reinterpret_cast<const float4 *>(p) + h);
+                    out[4 * h] = v.x;
+                    out[4 * h + 1] = v.y;
+                    out[4 * h + 2] = v.z;
+                    out[4 * h + 3] = v.w;
+                }
+            }
+            return;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < K; q++) out[q] = ld_x(p + q);
+}
+
+// Whether ld_xrow may use vector loads for X (host side): x and every row
+// start aligned to the vector width (16 bytes, 8 for FP32 with k = 2).
+inline int xrow_vec(const void *x, int64_t ldx, size_t value_bytes, int k) {
+    if (k < 2) return 0;
+    const size_t w = k * value_bytes >= 16 ? 16 : k * value_bytes;
+    return ((reinterpret_cast<uintptr_t>(x) | (uintptr_t)(ldx * (int64_t)value_bytes)) % w) == 0 ? 1 : 0;
+}
+
 template <typename V>
 __device__ __forceinline__ V axpby(V alpha, V sum, V beta, const V *y) {
     return beta == V(0) ? alpha * sum : alpha * sum + beta * *y;

@@ -332,7 +332,7 @@ __global__ void __launch_bounds__(kBlock, K == 1 ? (sizeof(V) == 4 ? 5 : 4) : 1)
     int64_t nnz, const int32_t *__restrict__ ri, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
     int32_t *__restrict__ carry_row, int32_t *__restrict__ has_end, V *__restrict__ carry_val,
-    V *__restrict__ head_val, int vec) {
+    V *__restrict__ head_val, int vec, int xvec) {
     constexpr unsigned kFull = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -352,9 +352,14 @@ __global__ void __launch_bounds__(kBlock, K == 1 ? (sizeof(V) == 4 ? 5 : 4) : 1)
     V xv[K <= 2 ? 8 : 1][K];
     if constexpr (K <= 2) {
 #pragma unroll
-        for (int u = 0; u < 8; u++)
+        for (int u = 0; u < 8; u++) {
+            if (u < nv) {
+                ld_xrow<V, K>(x, c[u], ldx, xvec != 0, xv[u]);
+            } else {
 #pragma unroll
-            for (int q = 0; q < K; q++) xv[u][q] = u < nv ? ld_x(x + (int64_t)c[u] * ldx + q) : V(0);
+                for (int q = 0; q < K; q++) xv[u][q] = V(0);
+            }
+        }
     }
     V seg[K], head[K];
 #pragma unroll
@@ -365,10 +370,14 @@ __global__ void __launch_bounds__(kBlock, K == 1 ? (sizeof(V) == 4 ? 5 : 4) : 1)
     for (int u = 0; u < 8; u++) {
         if (u < nv) {
             last_row = r[u];
+            if constexpr (K <= 2) {
 #pragma unroll
-            for (int q = 0; q < K; q++) {
-                if constexpr (K <= 2) seg[q] += a[u] * xv[u][q];
-                else seg[q] += a[u] * ld_x(x + (int64_t)c[u] * ldx + q);
+                for (int q = 0; q < K; q++) seg[q] += a[u] * xv[u][q];
+            } else {
+                V xr[K];
+                ld_xrow<V, K>(x, c[u], ldx, xvec != 0, xr);
+#pragma unroll
+                for (int q = 0; q < K; q++) seg[q] += a[u] * xr[q];
             }
             const int rn = u + 1 < nv ? r[u + 1] : next;
             if (rn != r[u]) {  // r[u] ends here
@@ -549,7 +558,7 @@ sspmv_status coo_pass(const sspmv_coo *A, Plan *p, V alpha, const V *x, int64_t 
                           reinterpret_cast<uintptr_t>(A->values)) & 15) == 0;
         coo_warp_kernel<V, K><<<grid_for(nt * 32, kBlock), kBlock, 0, cu(s)>>>(
             nnz, A->row_index, A->col_index, (const V *)A->values, x, ldx, alpha, beta, y, ldy, ints, ints + nt,
-            (V *)p->extra[which * 3 + 1], (V *)p->extra[which * 3 + 2], vec);
+            (V *)p->extra[which * 3 + 1], (V *)p->extra[which * 3 + 2], vec, xrow_vec(x, ldx, sizeof(V), K));
         SSPMV_LAUNCH_CHECK();
         if (nt > 1) {
             coo_fixup<V, K><<<grid_for(nt, 256), 256, 0, cu(s)>>>(nt, A->row_index, tile, ints, ints + nt,

@@ -209,6 +209,7 @@ __global__ void c5_transpose(int64_t nnz, int32_t p, int32_t sigma, int32_t omeg
 // ------------------------------------------------------------------ SpMV --
 struct C5View {
     int32_t m, n, p, sigma, byo, bao, np;
+    int32_t xvec;  // X rows aligned for vector loads (xrow_vec), set per call
     const int32_t *rp, *col;
     const void *val;
     const uint32_t *tp, *td;
@@ -302,9 +303,14 @@ __global__ void __launch_bounds__(kBlock) csr5_tile_kernel(C5View A, const V *__
                 }
             }
 #pragma unroll
-            for (int u = 0; u < kU; u++)
+            for (int u = 0; u < kU; u++) {
+                if (i0 + u < sigma) {
+                    ld_xrow<V, K>(x, cc[u], ldx, A.xvec != 0, xv[u]);
+                } else {
 #pragma unroll
-                for (int q = 0; q < K; q++) xv[u][q] = i0 + u < sigma ? ld_x(x + (int64_t)cc[u] * ldx + q) : V(0);
+                    for (int q = 0; q < K; q++) xv[u][q] = V(0);
+                }
+            }
 #pragma unroll
             for (int u = 0; u < kU; u++) {
                 const int i = i0 + u;
@@ -426,9 +432,10 @@ __global__ void __launch_bounds__(kBlock) csr5_rows_kernel(C5View A, int32_t tai
         for (int q = 0; q < K; q++) s[q] = V(0);
         for (int64_t j = s0 + lane; j < re; j += 32) {
             const V a = ld_stream(val + j);
-            const V *xp = x + (int64_t)ld_stream(A.col + j) * ldx;
+            V xr[K];
+            ld_xrow<V, K>(x, ld_stream(A.col + j), ldx, A.xvec != 0, xr);
 #pragma unroll
-            for (int q = 0; q < K; q++) s[q] += a * ld_x(xp + q);
+            for (int q = 0; q < K; q++) s[q] += a * xr[q];
         }
 #pragma unroll
         for (int q = 0; q < K; q++) s[q] = warp_sum(s[q]);
@@ -469,6 +476,7 @@ __global__ void csr5_fixup(int32_t ntiles, int64_t tile, const int32_t *__restri
 
 C5View view_of(const sspmv_csr5 *A) {
     C5View v;
+    v.xvec = 0;
     v.m = (int32_t)A->f.num_rows;
     v.n = (int32_t)A->f.num_cols;
     v.p = A->_p;
@@ -549,7 +557,8 @@ template <typename V, int K>
 sspmv_status csr5_pass(const sspmv_csr5 *A, Plan *pl, V alpha, const V *x, int64_t ldx, V beta, V *y, int64_t ldy,
                        sspmv_stream_t s) {
     SSPMV_TRY(ensure_c5_plan(A, pl, s));
-    const C5View v = view_of(A);
+    C5View v = view_of(A);
+    v.xvec = xrow_vec(x, ldx, sizeof(V), K);
     const int64_t p = std::max<int64_t>(A->_p, 1);
     int32_t *cr = (int32_t *)pl->extra[0], *he = cr + p;
     V *cv = (V *)pl->extra[1], *hv = (V *)pl->extra[2];

@@ -118,7 +118,7 @@ template <typename V, int K>
 __global__ void __launch_bounds__(kBlock) dia_spmv_kernel(int m, int n, int nd, int64_t stride,
                                                         const int64_t *__restrict__ offsets,
                                                         const V *__restrict__ data, const V *__restrict__ x,
-                                                        int64_t ldx, V alpha, V beta, V *__restrict__ y,
+                                                        int64_t ldx, int xvec, V alpha, V beta, V *__restrict__ y,
                                                         int64_t ldy) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
         V s[K];
@@ -138,16 +138,20 @@ __global__ void __launch_bounds__(kBlock) dia_spmv_kernel(int m, int n, int nd, 
 #pragma unroll
             for (int u = 0; u < 4; u++)
                 if (j[u] >= 0 && j[u] < n) {
+                    V xr[K];
+                    ld_xrow<V, K>(x, j[u], ldx, xvec != 0, xr);
 #pragma unroll
-                    for (int q = 0; q < K; q++) s[q] += a[u] * ld_x(x + j[u] * ldx + q);
+                    for (int q = 0; q < K; q++) s[q] += a[u] * xr[q];
                 }
         }
         for (; d < nd; d++) {
             const int64_t j = i + __ldg(offsets + d);
             if (j >= 0 && j < n) {
                 const V a = ld_stream(data + (int64_t)d * stride + i);
+                V xr[K];
+                ld_xrow<V, K>(x, j, ldx, xvec != 0, xr);
 #pragma unroll
-                for (int q = 0; q < K; q++) s[q] += a * ld_x(x + j * ldx + q);
+                for (int q = 0; q < K; q++) s[q] += a * xr[q];
             }
         }
         V *yp = y + i * ldy;
@@ -162,7 +166,7 @@ sspmv_status launch_dia(const sspmv_dia *A, V alpha, const V *x, int64_t ldx, V 
     const unsigned grid = grid_for(A->f.num_rows, kBlock, (int64_t)num_sms() * 16);
     dia_spmv_kernel<V, K><<<grid, kBlock, 0, cu(s)>>>((int)A->f.num_rows, (int)A->f.num_cols, A->complete_ndiags,
                                                       A->stride, A->diag_offsets, (const V *)A->diag_data, x, ldx,
-                                                      alpha, beta, y, ldy);
+                                                      xrow_vec(x, ldx, sizeof(V), K), alpha, beta, y, ldy);
     SSPMV_LAUNCH_CHECK();
     return SSPMV_OK;
 }

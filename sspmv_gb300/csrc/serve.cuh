@@ -37,7 +37,7 @@ struct BatchItem {
     int32_t m;
     int32_t num_chunks;
     int32_t vec;          // 16-byte aligned col_index / values: vector loads
-    int32_t pad;
+    int32_t xvec;         // X rows aligned for vector loads (xrow_vec)
 };
 
 struct BatchHeader {

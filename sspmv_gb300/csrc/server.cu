@@ -601,7 +601,7 @@ void Server::issue(Batch &b) {
         it.num_chunks = (int32_t)M.chunks;
         it.vec = ((reinterpret_cast<uintptr_t>(M.dev.csr.col_index) | reinterpret_cast<uintptr_t>(M.dev.csr.values)) &
                   15) == 0;
-        it.pad = 0;
+        it.xvec = xrow_vec(r->d_x, r->r.ldx, g >= 4 ? 8 : 4, r->r.k);
         group_tiles[g] += M.chunks;
         mask |= 1u << g;
     }

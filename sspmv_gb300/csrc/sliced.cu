@@ -54,8 +54,8 @@ constexpr int kSlots = 4;  // slots of a row whose loads are in flight together
 template <typename V, int K>
 __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
     int m, int C, const int64_t *__restrict__ chunk_ptr, const int32_t *__restrict__ reorder,
-    const int32_t *__restrict__ col, const V *__restrict__ val, const V *__restrict__ x, int64_t ldx, V alpha,
-    V beta, V *__restrict__ y, int64_t ldy, int64_t cap, const int32_t *__restrict__ ovf_id,
+    const int32_t *__restrict__ col, const V *__restrict__ val, const V *__restrict__ x, int64_t ldx, int xvec,
+    V alpha, V beta, V *__restrict__ y, int64_t ldy, int64_t cap, const int32_t *__restrict__ ovf_id,
     V *__restrict__ ovf_part) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t c = i / C;
@@ -80,8 +80,10 @@ __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
 #pragma unroll
             for (int u = 0; u < kSlots; u++)
                 if (cc[u] >= 0) {
+                    V xr[K];
+                    ld_xrow<V, K>(x, cc[u], ldx, xvec, xr);
 #pragma unroll
-                    for (int q = 0; q < K; q++) s[q] += aa[u] * ld_x(x + (int64_t)cc[u] * ldx + q);
+                    for (int q = 0; q < K; q++) s[q] += aa[u] * xr[q];
                 }
             if (cc[kSlots - 1] < 0) break;  // padding is a suffix of the row
         }
@@ -90,8 +92,10 @@ __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
                 const int cc = ld_stream(cp + k * C);
                 if (cc < 0) break;
                 const V aa = ld_stream(vp + k * C);
+                V xr[K];
+                ld_xrow<V, K>(x, cc, ldx, xvec, xr);
 #pragma unroll
-                for (int q = 0; q < K; q++) s[q] += aa * ld_x(x + (int64_t)cc * ldx + q);
+                for (int q = 0; q < K; q++) s[q] += aa * xr[q];
             }
         }
         if (wfull > w && ld_stream(cp + w * C) >= 0) {  // the row goes on past the cap: overflow
@@ -118,7 +122,7 @@ template <typename V, int K>
 __global__ void __launch_bounds__(kBlock) sliced_piece_kernel(int64_t npieces, const int4 *__restrict__ pieces,
                                                               const int32_t *__restrict__ ocol,
                                                               const V *__restrict__ oval, const V *__restrict__ x,
-                                                              int64_t ldx, V *__restrict__ partial) {
+                                                              int64_t ldx, int xvec, V *__restrict__ partial) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (warp >= npieces) return;
@@ -136,15 +140,20 @@ __global__ void __launch_bounds__(kBlock) sliced_piece_kernel(int64_t npieces, c
             aa[u] = ld_stream(oval + e + 32 * u);
         }
 #pragma unroll
-        for (int u = 0; u < 4; u++)
+        for (int u = 0; u < 4; u++) {
+            V xr[K];
+            ld_xrow<V, K>(x, cc[u], ldx, xvec, xr);
 #pragma unroll
-            for (int q = 0; q < K; q++) s[q] += aa[u] * ld_x(x + (int64_t)cc[u] * ldx + q);
+            for (int q = 0; q < K; q++) s[q] += aa[u] * xr[q];
+        }
     }
     for (; e < pc.z; e += 32) {
         const int cc = ld_stream(ocol + e);
         const V aa = ld_stream(oval + e);
+        V xr[K];
+        ld_xrow<V, K>(x, cc, ldx, xvec, xr);
 #pragma unroll
-        for (int q = 0; q < K; q++) s[q] += aa * ld_x(x + (int64_t)cc * ldx + q);
+        for (int q = 0; q < K; q++) s[q] += aa * xr[q];
     }
 #pragma unroll
     for (int q = 0; q < K; q++) s[q] = warp_sum(s[q]);
@@ -439,8 +448,9 @@ sspmv_status launch_sliced(const SlicedView &v, Plan *p, V alpha, const V *x, in
                            int64_t ldy, sspmv_stream_t s) {
     const int64_t nov = p ? p->extra_i[1] : 0;
     const unsigned grid = grid_for(v.m, kBlock, (int64_t)num_sms() * 16);
+    const int xvec = xrow_vec(x, ldx, sizeof(V), K);
     sliced_spmv_kernel<V, K><<<grid, kBlock, 0, cu(s)>>>(
-        (int)v.m, v.C, v.chunk_ptr, v.reorder, v.col, (const V *)v.val, x, ldx, alpha, beta, y, ldy,
+        (int)v.m, v.C, v.chunk_ptr, v.reorder, v.col, (const V *)v.val, x, ldx, xvec, alpha, beta, y, ldy,
         nov > 0 ? p->extra_i[2] : kNoCap, nov > 0 ? (const int32_t *)p->extra[8] : nullptr,
         nov > 0 ? (V *)p->extra[4] : nullptr);
     SSPMV_LAUNCH_CHECK();
@@ -450,7 +460,7 @@ sspmv_status launch_sliced(const SlicedView &v, Plan *p, V alpha, const V *x, in
         if (npieces > 0) {
             sliced_piece_kernel<V, K><<<grid_for(npieces * 32, kBlock), kBlock, 0, cu(s)>>>(
                 npieces, (const int4 *)p->extra[3], (const int32_t *)p->extra[5], (const V *)p->extra[6], x, ldx,
-                (V *)p->extra[7]);
+                xvec, (V *)p->extra[7]);
             SSPMV_LAUNCH_CHECK();
         }
         sliced_overflow_fixup<V, K><<<grid_for(nov, 256), 256, 0, cu(s)>>>(

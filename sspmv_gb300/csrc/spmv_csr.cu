@@ -257,7 +257,7 @@ __global__ void csr_merge_fixup(int64_t num_tiles, int m, const int32_t *__restr
 template <typename V, int K, int VS>
 __global__ void __launch_bounds__(kBlock) csr_vector_kernel(
     int m, const int32_t *__restrict__ row_offset, const int32_t *__restrict__ col_index,
-    const V *__restrict__ values, const V *__restrict__ x, int64_t ldx, V alpha, V beta,
+    const V *__restrict__ values, const V *__restrict__ x, int64_t ldx, int xvec, V alpha, V beta,
     V *__restrict__ y, int64_t ldy) {
     constexpr int kRowsPerWarp = 32 / VS;
     const int lane = threadIdx.x & 31;
@@ -281,15 +281,20 @@ __global__ void __launch_bounds__(kBlock) csr_vector_kernel(
                     a[u] = ld_stream(values + j + u * VS);
                 }
 #pragma unroll
-                for (int u = 0; u < 4; u++)
+                for (int u = 0; u < 4; u++) {
+                    V xr[K];
+                    ld_xrow<V, K>(x, c[u], ldx, xvec != 0, xr);
 #pragma unroll
-                    for (int r = 0; r < K; r++) s[r] += a[u] * ld_x(x + (int64_t)c[u] * ldx + r);
+                    for (int r = 0; r < K; r++) s[r] += a[u] * xr[r];
+                }
             }
             for (; j < re; j += VS) {
                 const int c = ld_stream(col_index + j);
                 const V a = ld_stream(values + j);
+                V xr[K];
+                ld_xrow<V, K>(x, c, ldx, xvec != 0, xr);
 #pragma unroll
-                for (int r = 0; r < K; r++) s[r] += a * ld_x(x + (int64_t)c * ldx + r);
+                for (int r = 0; r < K; r++) s[r] += a * xr[r];
             }
         }
 #pragma unroll
@@ -335,7 +340,8 @@ sspmv_status launch_vector_vs(const sspmv_csr *A, V alpha, const V *x, int64_t l
     const int64_t warps = (m + (32 / VS) - 1) / (32 / VS);
     const unsigned grid = grid_for(warps * 32, kBlock, (int64_t)num_sms() * 16);
     csr_vector_kernel<V, K, VS><<<grid, kBlock, 0, cu(s)>>>((int)m, A->row_offset, A->col_index,
-                                                            (const V *)A->values, x, ldx, alpha, beta, y, ldy);
+                                                            (const V *)A->values, x, ldx,
+                                                            xrow_vec(x, ldx, sizeof(V), K), alpha, beta, y, ldy);
     SSPMV_LAUNCH_CHECK();
     return SSPMV_OK;
 }
@@ -588,7 +594,7 @@ __device__ __forceinline__ void stream_chunk_lanes(
     int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
     const int32_t *__restrict__ row_start, const int64_t w, const int64_t slot, int32_t *__restrict__ carry_row,
-    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val, int vec) {
+    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val, int vec, int xvec) {
     constexpr unsigned kFull = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int64_t j0 = w * kStreamChunk;
@@ -614,9 +620,14 @@ __device__ __forceinline__ void stream_chunk_lanes(
     V xv[K <= 2 ? 8 : 1][K];
     if constexpr (K <= 2) {
 #pragma unroll
-        for (int u = 0; u < 8; u++)
+        for (int u = 0; u < 8; u++) {
+            if (u < nv) {
+                ld_xrow<V, K>(x, c[u], ldx, xvec != 0, xv[u]);
+            } else {
 #pragma unroll
-            for (int q = 0; q < K; q++) xv[u][q] = u < nv ? ld_x(x + (int64_t)c[u] * ldx + q) : V(0);
+                for (int q = 0; q < K; q++) xv[u][q] = V(0);
+            }
+        }
     }
     if (e0 == 0 && nv > 0) {  // empty rows before the first nonzero
         for (int r2 = 0; r2 < r; r2++) {
@@ -636,10 +647,14 @@ __device__ __forceinline__ void stream_chunk_lanes(
         if (u < nv) {
             const int64_t e = e0 + u;
             while (rend <= e) rend = __ldg(rp + (++r) + 1);  // skip empty rows
+            if constexpr (K <= 2) {
 #pragma unroll
-            for (int q = 0; q < K; q++) {
-                if constexpr (K <= 2) seg[q] += a[u] * xv[u][q];
-                else seg[q] += a[u] * ld_x(x + (int64_t)c[u] * ldx + q);
+                for (int q = 0; q < K; q++) seg[q] += a[u] * xv[u][q];
+            } else {
+                V xr[K];
+                ld_xrow<V, K>(x, c[u], ldx, xvec != 0, xr);
+#pragma unroll
+                for (int q = 0; q < K; q++) seg[q] += a[u] * xr[q];
             }
             last_row = r;
             last_open = rend != e + 1;
@@ -728,7 +743,7 @@ __device__ __forceinline__ void stream_chunk_fast(
     int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy, const int ra,
     const int last, const int64_t w, const int64_t slot, int32_t *__restrict__ carry_row,
-    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val, int vec,
+    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val, int vec, int xvec,
     uint32_t *__restrict__ sbits) {
     constexpr unsigned kFull = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -770,9 +785,14 @@ __device__ __forceinline__ void stream_chunk_fast(
     V xv[K <= 2 ? 8 : 1][K];
     if constexpr (K <= 2) {
 #pragma unroll
-        for (int u = 0; u < 8; u++)
+        for (int u = 0; u < 8; u++) {
+            if (u < nv) {
+                ld_xrow<V, K>(x, c[u], ldx, xvec != 0, xv[u]);
+            } else {
 #pragma unroll
-            for (int q = 0; q < K; q++) xv[u][q] = u < nv ? ld_x(x + (int64_t)c[u] * ldx + q) : V(0);
+                for (int q = 0; q < K; q++) xv[u][q] = V(0);
+            }
+        }
     }
     int r = ra + pos;
     V seg[K], head[K];
@@ -783,10 +803,14 @@ __device__ __forceinline__ void stream_chunk_fast(
 #pragma unroll
     for (int u = 0; u < 8; u++) {
         if (u < nv) {
+            if constexpr (K <= 2) {
 #pragma unroll
-            for (int q = 0; q < K; q++) {
-                if constexpr (K <= 2) seg[q] += a[u] * xv[u][q];
-                else seg[q] += a[u] * ld_x(x + (int64_t)c[u] * ldx + q);
+                for (int q = 0; q < K; q++) seg[q] += a[u] * xv[u][q];
+            } else {
+                V xr[K];
+                ld_xrow<V, K>(x, c[u], ldx, xvec != 0, xr);
+#pragma unroll
+                for (int q = 0; q < K; q++) seg[q] += a[u] * xr[q];
             }
             last_row = r;
             last_open = !((ends >> u) & 1u);
@@ -866,8 +890,8 @@ __device__ __forceinline__ void stream_chunk(
     int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
     const int32_t *__restrict__ row_start, const int64_t w, const int64_t slot, int32_t *__restrict__ carry_row,
-    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val, int vec, int no_empty,
-    uint32_t *__restrict__ sbits) {
+    int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val, int vec, int xvec,
+    int no_empty, uint32_t *__restrict__ sbits) {
     if constexpr (K == 8 && sizeof(V) == 8) {
         stream_chunk_cols<V, K, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, slot, carry_row,
                                    has_end, carry_val, head_val);
@@ -876,11 +900,11 @@ __device__ __forceinline__ void stream_chunk(
             const int ra = __ldg(row_start + w);
             const int last = min(__ldg(row_start + w + 1), m - 1) + 1;
             stream_chunk_fast<V, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, ra, last, w, slot, carry_row,
-                                    has_end, carry_val, head_val, vec, sbits);
+                                    has_end, carry_val, head_val, vec, xvec, sbits);
             return;
         }
         stream_chunk_lanes<V, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, slot, carry_row,
-                                 has_end, carry_val, head_val, vec);
+                                 has_end, carry_val, head_val, vec, xvec);
     }
 }
 
@@ -888,14 +912,14 @@ __device__ __forceinline__ void stream_chunk(
     __shared__ uint32_t s_bits[kBlock / 32][33];                                                          \
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;                              \
     stream_chunk<V, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, w, carry_row, has_end, \
-                       carry_val, head_val, vec, no_empty, s_bits[threadIdx.x >> 5]);
+                       carry_val, head_val, vec, xvec, no_empty, s_bits[threadIdx.x >> 5]);
 
 template <typename V, int K>
 __global__ void __launch_bounds__(kBlock) csr_stream_kernel(
     int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
     const int32_t *__restrict__ row_start, int32_t *__restrict__ carry_row, int32_t *__restrict__ has_end,
-    V *__restrict__ carry_val, V *__restrict__ head_val, int vec, int no_empty) {
+    V *__restrict__ carry_val, V *__restrict__ head_val, int vec, int xvec, int no_empty) {
     SSPMV_STREAM_KERNEL_BODY
 }
 
@@ -906,7 +930,7 @@ __global__ void __launch_bounds__(kBlock, 6) csr_stream_kernel_occ6(
     int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
     const int32_t *__restrict__ row_start, int32_t *__restrict__ carry_row, int32_t *__restrict__ has_end,
-    V *__restrict__ carry_val, V *__restrict__ head_val, int vec, int no_empty) {
+    V *__restrict__ carry_val, V *__restrict__ head_val, int vec, int xvec, int no_empty) {
     SSPMV_STREAM_KERNEL_BODY
 }
 #undef SSPMV_STREAM_KERNEL_BODY
@@ -978,16 +1002,17 @@ sspmv_status launch_stream(const sspmv_csr *A, Plan *p, V alpha, const V *x, int
     const int vec = ((reinterpret_cast<uintptr_t>(A->col_index) | reinterpret_cast<uintptr_t>(A->values)) & 15) == 0;
     const unsigned grid = grid_for(nt * 32, kBlock);
     const int no_empty = p->extra_i[1] == 0 ? 1 : 0;
+    const int xvec = xrow_vec(x, ldx, sizeof(V), K);
     if constexpr (sizeof(V) == 4 && K == 1)
         csr_stream_kernel_occ6<V, K><<<grid, kBlock, 0, cu(s)>>>(
             (int)A->f.num_rows, A->f.num_nnzs, A->row_offset, A->col_index, (const V *)A->values, x, ldx, alpha,
             beta, y, ldy, (const int32_t *)p->extra[0], ints, ints + nt, (V *)p->extra[2], (V *)p->extra[3], vec,
-            no_empty);
+            xvec, no_empty);
     else
         csr_stream_kernel<V, K><<<grid, kBlock, 0, cu(s)>>>(
             (int)A->f.num_rows, A->f.num_nnzs, A->row_offset, A->col_index, (const V *)A->values, x, ldx, alpha,
             beta, y, ldy, (const int32_t *)p->extra[0], ints, ints + nt, (V *)p->extra[2], (V *)p->extra[3], vec,
-            no_empty);
+            xvec, no_empty);
     SSPMV_LAUNCH_CHECK();
     if (nt > 1) {
         csr_stream_fixup<V, K><<<grid_for(nt, 256), 256, 0, cu(s)>>>(nt, A->row_offset, ints, ints + nt,
@@ -1031,7 +1056,7 @@ __global__ void __launch_bounds__(kBlock) csr_batch_kernel(int g, const BatchHea
         const BatchItem *q = items + batch_item_of(items, n, gc);
         stream_chunk<V, K>(q->m, q->nnz, q->row_offset, q->col_index, (const V *)q->values, (const V *)q->x, q->ldx,
                            (V)q->alpha, (V)q->beta, (V *)q->y, q->ldy, q->row_start, gc - q->chunk_begin, base + gc,
-                           carry_row, has_end, carry_val, head_val, q->vec, 0, nullptr);
+                           carry_row, has_end, carry_val, head_val, q->vec, q->xvec, 0, nullptr);
     }
 }
 
