@@ -302,6 +302,11 @@ def run_gpu(args, rank, world):
             if key not in ceiling:
                 ceiling[key] = L.gather_ceiling(np_dtype(c["dt"]), c["cols"], min(c["nnz"], 1 << 28))[0]
             pc["gather_frac"] = round(c["nnz"] / (pc["ms"] * 1e-3) / ceiling[key], 4)
+        # FP64: one FMA per nonzero against the device's measured FP64 FMA rate
+        fma_rate = L.fp64_ceiling()
+        for c, pc in zip(cases, per_case):
+            if c["dt"] == "f64":
+                pc["fp64_frac"] = round(c["nnz"] / (pc["ms"] * 1e-3) / fma_rate, 4)
         key = (dc["fam"], dc["dt"])
         rate = ceiling.get(key) or L.gather_ceiling(np_dtype(dc["dt"]), dc["cols"], min(dc["nnz"], 1 << 28))[0]
         kernel_rate = dc["nnz"] / (per_case[dom]["ms"] * 1e-3)
@@ -310,6 +315,11 @@ def run_gpu(args, rank, world):
             "frac": round(kernel_rate / rate, 4),
             "what": "one x gather per nonzero; ceiling = random gathers from a vector of the same size, "
                     "indices streamed (sspmv_gather_ceiling)"}
+        if dc["dt"] == "f64":
+            roofline["fp64_ceiling"] = {
+                "ceiling_fmas_per_s": round(fma_rate, 1), "achieved_fmas_per_s": round(kernel_rate, 1),
+                "frac": round(kernel_rate / fma_rate, 4),
+                "what": "one FP64 FMA per nonzero; ceiling = independent FMA chains (sspmv_fp64_ceiling)"}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(hosts, families, dtypes, fmts, budget_s=15.0)

@@ -217,6 +217,11 @@ int64_t sspmv_launch_count(void);
  * (no reference counterpart); allocates and frees its own buffers. */
 sspmv_status sspmv_gather_ceiling(int32_t value_type, int64_t num_cols, int64_t num_gathers,
                                   double *gathers_per_second, double *checksum, sspmv_stream_t stream);
+/* Measured FP64 fused multiply-add rate of the device (independent chains,
+ * best of 5 launches after 3 warm-up ones), in FMAs per second: the bound of
+ * FP64 SpMV (one FMA per nonzero) where neither bytes nor gathers bind.
+ * A measurement utility of this library (no reference counterpart). */
+sspmv_status sspmv_fp64_ceiling(double *fmas_per_second, sspmv_stream_t stream);
 /* Selects the SpMV kernel of a matrix (pass &A->f): kernel_flag as in each
  * format's LeSpMV entry, param a kernel parameter (0 lets the library
  * choose): CSR vector kernel: lanes per row 2..32; S-ELL, SELL-c-sigma,

@@ -122,6 +122,7 @@ _SIGS = {
     "sspmv_version": (C.c_char_p, []),
     "sspmv_launch_count": (_i64, []),
     "sspmv_gather_ceiling": (_st, [_i32, _i64, _i64, C.POINTER(_d), C.POINTER(_d), _vp]),
+    "sspmv_fp64_ceiling": (_st, [C.POINTER(_d), _vp]),
     "sspmv_set_kernel": (_st, [C.POINTER(Features), _i32, _i32]),
     "sspmv_csr_create": (_st, [C.POINTER(Csr), _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp]),
     "sspmv_csr_wrap": (_st, [C.POINTER(Csr), _i32, _i64, _i64, _i64, _vp, _vp, _vp]),

@@ -1,4 +1,5 @@
-// calibrate.cu -- the measured ceiling of random gathers from the x vector.
+// calibrate.cu -- measured ceilings the SpMV kernels are set against: random
+// gathers from the x vector, and FP64 FMA throughput.
 //
 // SpMV on matrices whose column indices are spread at random (uniform,
 // power-law) is bound by the x gathers, not by HBM: every gathered element
@@ -7,7 +8,9 @@
 // runs that access pattern alone -- indices streamed once with evict-first
 // loads, 8 read-only gathers in flight per lane, one sum per thread -- so
 // a kernel's gather rate can be set against what the GPU delivers for the
-// same pattern.
+// same pattern.  GB300's FP64 rate is low enough (~1 FP64 FMA per 16 bytes of
+// HBM bandwidth) that FP64 SpMV, one FMA per nonzero, can be bound by its FMAs
+// rather than by its bytes: dfma_kernel measures that rate.
 #include "common.cuh"
 
 #include <algorithm>
@@ -59,10 +62,58 @@ __global__ void __launch_bounds__(kBlockG) gather_kernel(const V *__restrict__ x
     out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = acc;
 }
 
+// FP64 FMA throughput: eight independent chains per thread, `iters` steps.
+__global__ void __launch_bounds__(kBlockG) dfma_kernel(int64_t iters, double b, double c, double *__restrict__ out) {
+    double a[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) a[u] = 1.0 + 0.125 * u + 1e-3 * (threadIdx.x & 7);
+    for (int64_t i = 0; i < iters; i++) {
+#pragma unroll
+        for (int u = 0; u < 8; u++) a[u] = fma(a[u], b, c);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int u = 0; u < 8; u++) s += a[u];
+    out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace
 }  // namespace sspmv
 
 using namespace sspmv;
+
+extern "C" sspmv_status sspmv_fp64_ceiling(double *fmas_per_second, sspmv_stream_t stream) {
+    if (!fmas_per_second) return fail(SSPMV_INVALID_ARG, "fp64 ceiling: null output");
+    const unsigned grid = (unsigned)(num_sms() * 8);
+    const int64_t iters = 4096;
+    double *out = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float best = 0.f;
+    auto body = [&]() -> sspmv_status {
+        SSPMV_TRY(dalloc(&out, (size_t)grid * kBlockG, stream));
+        SSPMV_CUDA_TRY(cudaEventCreate(&e0));
+        SSPMV_CUDA_TRY(cudaEventCreate(&e1));
+        for (int rep = 0; rep < 8; rep++) {  // 3 warm-up launches, best of 5 timed
+            SSPMV_CUDA_TRY(cudaEventRecord(e0, cu(stream)));
+            dfma_kernel<<<grid, kBlockG, 0, cu(stream)>>>(iters, 0.999999, 1e-9, out);
+            SSPMV_LAUNCH_CHECK();
+            SSPMV_CUDA_TRY(cudaEventRecord(e1, cu(stream)));
+            SSPMV_CUDA_TRY(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            SSPMV_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+            if (rep >= 3 && (best == 0.f || ms < best)) best = ms;
+        }
+        return SSPMV_OK;
+    };
+    const sspmv_status st = body();
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    dfree(out, stream);
+    if (st != SSPMV_OK) return st;
+    cudaStreamSynchronize(cu(stream));
+    *fmas_per_second = (double)grid * kBlockG * (double)iters * 8.0 / ((double)best * 1e-3);
+    return SSPMV_OK;
+}
 
 extern "C" sspmv_status sspmv_gather_ceiling(int32_t value_type, int64_t num_cols, int64_t num_gathers,
                                              double *gathers_per_second, double *checksum, sspmv_stream_t stream) {

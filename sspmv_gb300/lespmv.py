@@ -342,6 +342,14 @@ def gather_ceiling(dtype, num_cols: int, num_gathers: int, stream=None) -> tuple
     return rate.value, chk.value
 
 
+def fp64_ceiling(stream=None) -> float:
+    """Measured FP64 FMA rate of the device (FMAs/s), the bound of FP64 SpMV
+    where neither bytes nor gathers bind (one FMA per nonzero)."""
+    rate = C.c_double(0.0)
+    call("sspmv_fp64_ceiling", C.byref(rate), _stream(stream))
+    return rate.value
+
+
 def read_csr_matrix(path: str, precision: int = 64) -> HostCSR:
     """read_csr_matrix (utils/sparse_io.cpp:180-204) on the host."""
     vt = F64 if precision == 64 else F32

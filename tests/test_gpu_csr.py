@@ -112,3 +112,8 @@ def test_gather_ceiling_checksum(dt):
     ref = float(x[idx].astype(np.float64).sum())
     assert rate > 0
     assert abs(chk - ref) <= 1e-6 * ref
+
+
+def test_fp64_ceiling_positive():
+    from sspmv_gb300.lespmv import fp64_ceiling
+    assert fp64_ceiling() > 1e9
