@@ -274,6 +274,9 @@ sspmv_status sspmv_LeSpMV_csr_noalloc(double alpha, const sspmv_csr *A, const vo
 /* ---------------- ELL ---------------- */
 /* csr_to_ell (include/sparse_conversion.h:187-248) */
 sspmv_status sspmv_csr_to_ell(const sspmv_csr *csr, int32_t ld, sspmv_ell *out, sspmv_stream_t stream);
+/* coo_to_ell (include/sparse_conversion.h:94-142): each row's entries in COO
+ * order; ld is ignored and the result is RowMajor, as in the reference. */
+sspmv_status sspmv_coo_to_ell(const sspmv_coo *coo, int32_t ld, sspmv_ell *out, sspmv_stream_t stream);
 /* LeSpMV_ell (src/spmv_ell.cpp:225-247): one thread per row over the
  * column-major slots, stopping at the row's first padding slot. */
 sspmv_status sspmv_LeSpMV_ell(double alpha, const sspmv_ell *A, const void *x, double beta, void *y,
@@ -442,6 +445,12 @@ sspmv_status sspmv_csr_grx_features(const sspmv_csr *A, int32_t tile_blocks, int
  * with NULL arrays to get sizes, then with buffers of those sizes. */
 sspmv_status sspmv_read_mtx(const char *path, int32_t value_type, int64_t *num_rows, int64_t *num_cols,
                             int64_t *num_nnzs, int32_t *row_offset, int32_t *col_index, void *values);
+/* read_coo_matrix (utils/sparse_io.cpp:27-163): the triplets in file order
+ * (0-based; symmetric files: each off-diagonal entry followed by its
+ * mirror; pattern values 1.0), into host arrays of num_nnzs entries.  Call
+ * with row_index == NULL to get the sizes first. */
+sspmv_status sspmv_read_mtx_coo(const char *path, int32_t value_type, int64_t *num_rows, int64_t *num_cols,
+                                int64_t *num_nnzs, int32_t *row_index, int32_t *col_index, void *values);
 
 /* Writes a CSR matrix as "matrix coordinate real general" (1-based, %.17g),
  * a file the reference's read_csr_matrix reads back bit-exactly. */

@@ -150,6 +150,29 @@ extern "C" sspmv_status sspmv_read_mtx(const char *path, int32_t value_type, int
     return SSPMV_OK;
 }
 
+extern "C" sspmv_status sspmv_read_mtx_coo(const char *path, int32_t value_type, int64_t *num_rows,
+                                           int64_t *num_cols, int64_t *num_nnzs, int32_t *row_index,
+                                           int32_t *col_index, void *values) {
+    if (!path || !num_rows || !num_cols || !num_nnzs) return fail(SSPMV_INVALID_ARG, "null argument");
+    if (value_type != SSPMV_F32 && value_type != SSPMV_F64) return fail(SSPMV_INVALID_ARG, "bad value_type");
+    Triplets t;
+    sspmv_status st = read_triplets(path, t);
+    if (st != SSPMV_OK) return st;
+    const int64_t nnz = (int64_t)t.r.size();
+    *num_rows = t.m;
+    *num_cols = t.n;
+    *num_nnzs = nnz;
+    if (!row_index) return SSPMV_OK;  // size query
+    if (nnz > 0 && (!col_index || !values)) return fail(SSPMV_INVALID_ARG, "null output array");
+    for (int64_t k = 0; k < nnz; k++) {  // file order, mirrors right after their entries
+        row_index[k] = t.r[(size_t)k];
+        col_index[k] = t.c[(size_t)k];
+        if (value_type == SSPMV_F64) ((double *)values)[k] = t.v[(size_t)k];
+        else ((float *)values)[k] = (float)t.v[(size_t)k];
+    }
+    return SSPMV_OK;
+}
+
 extern "C" sspmv_status sspmv_write_mtx(const char *path, int64_t num_rows, int64_t num_cols,
                                         const int32_t *row_offset, const int32_t *col_index, const double *values) {
     if (!path || !row_offset) return fail(SSPMV_INVALID_ARG, "null argument");

@@ -743,6 +743,20 @@ double sliced_bytes(const sspmv_features *f, int64_t nchunks, bool reorder, int3
 }  // namespace
 
 // =================================================================== ELL ===
+// coo_to_ell (include/sparse_conversion.h:94-142): row counts, then each row's
+// entries in COO order.  The same slab as csr_to_ell on the COO's stable
+// row sort (coo_to_csr keeps each row's entries in COO order), so that is how
+// it is built.  Like the reference it ignores ld (it always sets RowMajor).
+extern "C" sspmv_status sspmv_coo_to_ell(const sspmv_coo *coo, int32_t ld, sspmv_ell *out, sspmv_stream_t s) {
+    if (!coo || !out) return fail(SSPMV_INVALID_ARG, "null argument");
+    (void)ld;
+    sspmv_csr csr;
+    SSPMV_TRY(sspmv_coo_to_csr(coo, &csr, s));
+    const sspmv_status st = sspmv_csr_to_ell(&csr, SSPMV_ROW_MAJOR, out, s);
+    sspmv_delete_csr(&csr);
+    return st;
+}
+
 extern "C" sspmv_status sspmv_csr_to_ell(const sspmv_csr *csr, int32_t ld, sspmv_ell *out, sspmv_stream_t s) {
     SSPMV_TRY(check_csr(csr));
     if (!out) return fail(SSPMV_INVALID_ARG, "null output");

@@ -245,6 +245,14 @@ def coo_to_csr(coo: COO_Matrix, stream=None) -> CSR_Matrix:
     return CSR_Matrix(s)
 
 
+def coo_to_ell(coo: COO_Matrix, ld: int = RowMajor, stream=None) -> ELL_Matrix:
+    """coo_to_ell (include/sparse_conversion.h:94-142): each row's entries in
+    COO order; ld is ignored (RowMajor), as in the reference."""
+    s = _lib.Ell()
+    call("sspmv_coo_to_ell", coo.ref(), int(ld), C.byref(s), _stream(stream))
+    return ELL_Matrix(s)
+
+
 def csr_to_dia(csr: CSR_Matrix, max_diags: int = 0, alignment: int = 0, stream=None) -> DIA_Matrix:
     """csr_to_dia (include/sparse_conversion.h:612-766); SSPMVError status 2
     (SSPMV_INFEASIBLE) above max_diags."""
@@ -361,6 +369,81 @@ def read_csr_matrix(path: str, precision: int = 64) -> HostCSR:
     call("sspmv_read_mtx", str(path).encode(), vt, C.byref(m), C.byref(n), C.byref(nnz),
          rp.ctypes.data_as(C.c_void_p), col.ctypes.data_as(C.c_void_p), val.ctypes.data_as(C.c_void_p))
     return HostCSR(int(m.value), int(n.value), rp, col, val)
+
+
+def read_coo_triplets(path: str, precision: int = 64):
+    """The .mtx triplets in file order (read_coo_matrix's order, symmetric
+    mirrors right after their entries): (num_rows, num_cols, rows, cols, vals)."""
+    vt = F64 if precision == 64 else F32
+    m, n, nnz = C.c_int64(), C.c_int64(), C.c_int64()
+    call("sspmv_read_mtx_coo", str(path).encode(), vt, C.byref(m), C.byref(n), C.byref(nnz), None, None, None)
+    ri = np.empty(nnz.value, np.int32)
+    ci = np.empty(nnz.value, np.int32)
+    val = np.empty(nnz.value, np.float64 if vt == F64 else np.float32)
+    call("sspmv_read_mtx_coo", str(path).encode(), vt, C.byref(m), C.byref(n), C.byref(nnz),
+         ri.ctypes.data_as(C.c_void_p), ci.ctypes.data_as(C.c_void_p), val.ctypes.data_as(C.c_void_p))
+    return int(m.value), int(n.value), ri, ci, val
+
+
+# Readers of the reference's sparse_io.h: .mtx -> device matrix of a format
+# (utils/sparse_io.cpp: CSR then csr_to_<fmt>; ELL through COO).
+def read_coo_matrix(path: str, precision: int = 64, stream=None) -> COO_Matrix:
+    """read_coo_matrix (utils/sparse_io.cpp:27-163): entries in file order."""
+    return coo_from_host(*read_coo_triplets(path, precision), stream=stream)
+
+
+def read_csr_device(path: str, precision: int = 64, stream=None) -> CSR_Matrix:
+    """read_csr_matrix (utils/sparse_io.cpp:180-204) onto the device."""
+    return csr_from_host(read_csr_matrix(path, precision), stream)
+
+
+def _read_then(path, precision, convert, stream):
+    csr = read_csr_device(path, precision, stream)
+    try:
+        return convert(csr)
+    finally:
+        csr.delete()
+
+
+def read_ell_matrix(path: str, ld: int = RowMajor, precision: int = 64, stream=None) -> ELL_Matrix:
+    """read_ell_matrix (utils/sparse_io.cpp:273-299): read_coo_matrix, then coo_to_ell."""
+    coo = read_coo_matrix(path, precision, stream)
+    try:
+        return coo_to_ell(coo, ld, stream)
+    finally:
+        coo.delete()
+
+
+def read_dia_matrix(path: str, max_diags: int = 0, alignment: int = 0, precision: int = 64, stream=None):
+    """read_dia_matrix (utils/sparse_io.cpp:315-329)."""
+    return _read_then(path, precision, lambda c: csr_to_dia(c, max_diags, alignment, stream), stream)
+
+
+def read_bsr_matrix(path: str, blockDimRow: int = 0, blockDimCol: int = 0, precision: int = 64, stream=None):
+    """read_bsr_matrix (utils/sparse_io.cpp:213-227)."""
+    return _read_then(path, precision, lambda c: csr_to_bsr(c, blockDimRow, blockDimCol, stream), stream)
+
+
+def read_csr5_matrix(path: str, precision: int = 64, stream=None):
+    """read_csr5_matrix (utils/sparse_io.cpp:243-258)."""
+    return _read_then(path, precision, lambda c: csr_to_csr5(c, 0, 0, stream), stream)
+
+
+def read_sell_matrix(path: str, chunkwidth: int = 0, alignment: int = 0, precision: int = 64, stream=None):
+    """read_sell_matrix (utils/sparse_io.cpp:347-362)."""
+    return _read_then(path, precision, lambda c: csr_to_sell(c, chunkwidth, alignment, stream), stream)
+
+
+def read_sell_c_sigma_matrix(path: str, slicewidth: int = 0, chunkwidth: int = 0, alignment: int = 0,
+                             precision: int = 64, stream=None):
+    """read_sell_c_sigma_matrix (utils/sparse_io.cpp:370-384)."""
+    return _read_then(path, precision, lambda c: csr_to_sell_c_sigma(c, slicewidth, chunkwidth, alignment, stream),
+                      stream)
+
+
+def read_sell_c_R_matrix(path: str, chunkwidth: int = 0, alignment: int = 0, precision: int = 64, stream=None):
+    """read_sell_c_R_matrix (utils/sparse_io.cpp:393-407)."""
+    return _read_then(path, precision, lambda c: csr_to_sell_c_R(c, chunkwidth, alignment, stream), stream)
 
 
 def write_mtx(path: str, A: HostCSR) -> None:

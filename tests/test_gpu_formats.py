@@ -283,3 +283,38 @@ def test_dia_converter_mixed_warps(oracle_lib):
     for name, arr in ref.items():
         if isinstance(arr, np.ndarray):
             assert np.array_equal(out[name].view(np.uint8), arr.view(np.uint8)), name
+
+
+def test_readers_and_coo_to_ell(tmp_path, oracle_lib):
+    """read_<fmt>_matrix (a .mtx through CSR, ELL through COO) give the
+    arrays of the converters on read_csr_matrix; coo_to_ell on an unsorted COO
+    equals csr_to_ell after coo_to_csr (each row in COO order)."""
+    from sspmv_gb300 import lespmv as L
+    from sspmv_gb300 import synth
+    A = synth.generate(synth.powerlaw(3000, 1.8, 8.0, 200, 0.05), 2)
+    p = tmp_path / "a.mtx"
+    L.write_mtx(str(p), A)
+    csr = L.csr_from_host(L.read_csr_matrix(str(p)))
+    pairs = [
+        (L.read_ell_matrix(str(p)), L.csr_to_ell(csr, L.RowMajor)),
+        (L.read_sell_matrix(str(p), 8, 4), L.csr_to_sell(csr, 8, 4)),
+        (L.read_sell_c_sigma_matrix(str(p), 256, 8, 0), L.csr_to_sell_c_sigma(csr, 256, 8, 0)),
+        (L.read_sell_c_R_matrix(str(p), 16, 0), L.csr_to_sell_c_R(csr, 16, 0)),
+        (L.read_bsr_matrix(str(p), 4, 4), L.csr_to_bsr(csr, 4, 4)),
+        (L.read_csr5_matrix(str(p)), L.csr_to_csr5(csr)),
+    ]
+    for got, ref in pairs:
+        a, b = got.export(), ref.export()
+        for k in b:
+            if isinstance(b[k], np.ndarray):
+                assert np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)), (type(got).__name__, k)
+    coo = L.read_coo_matrix(str(p))
+    assert coo.num_nnzs == A.nnz
+    rows = np.repeat(np.arange(A.num_rows, dtype=np.int32), np.diff(A.row_offset))
+    perm = np.random.default_rng(3).permutation(A.nnz)
+    ucoo = L.coo_from_host(A.num_rows, A.num_cols, rows[perm], A.col_index[perm], A.values[perm])
+    e1 = L.coo_to_ell(ucoo).export()
+    e2 = L.csr_to_ell(L.coo_to_csr(ucoo), L.RowMajor).export()
+    for k in e2:
+        if isinstance(e2[k], np.ndarray):
+            assert np.array_equal(e1[k].view(np.uint8), e2[k].view(np.uint8)), k
