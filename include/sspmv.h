@@ -451,6 +451,12 @@ sspmv_status sspmv_read_mtx(const char *path, int32_t value_type, int64_t *num_r
  * with row_index == NULL to get the sizes first. */
 sspmv_status sspmv_read_mtx_coo(const char *path, int32_t value_type, int64_t *num_rows, int64_t *num_cols,
                                 int64_t *num_nnzs, int32_t *row_index, int32_t *col_index, void *values);
+/* sum_csr_duplicates (include/sparse_operation.h:22-73), the compact step of
+ * coo_to_csr / read_csr_matrix(path, compact = true): in place on host CSR
+ * arrays; per row equal columns summed, columns in reverse order of first
+ * appearance, zero sums dropped; row_offset rewritten, *num_nnzs set. */
+sspmv_status sspmv_sum_csr_duplicates(int32_t value_type, int64_t num_rows, int64_t num_cols, int32_t *row_offset,
+                                      int32_t *col_index, void *values, int64_t *num_nnzs);
 
 /* Writes a CSR matrix as "matrix coordinate real general" (1-based, %.17g),
  * a file the reference's read_csr_matrix reads back bit-exactly. */

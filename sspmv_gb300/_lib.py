@@ -173,6 +173,7 @@ _SIGS.update(_format_sigs("csr5", Csr5, [_i32, _i32], [_vp, _vp, _vp, _vp, _vp, 
 _SIGS["sspmv_coo_create"] = (_st, [C.POINTER(Coo), _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp])
 _SIGS["sspmv_coo_to_csr"] = (_st, [C.POINTER(Coo), C.POINTER(Csr), _vp])
 _SIGS["sspmv_coo_to_ell"] = (_st, [C.POINTER(Coo), _i32, C.POINTER(Ell), _vp])
+_SIGS["sspmv_sum_csr_duplicates"] = (_st, [_i32, _i64, _i64, _vp, _vp, _vp, C.POINTER(_i64)])
 _SIGS["sspmv_read_mtx_coo"] = (_st, [C.c_char_p, _i32, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64), _vp, _vp,
                                      _vp])
 _SIGS["sspmv_csr_count_blocks"] = (_st, [C.POINTER(Csr), _i32, _i32, C.POINTER(_i64), _vp])

@@ -173,6 +173,57 @@ extern "C" sspmv_status sspmv_read_mtx_coo(const char *path, int32_t value_type,
     return SSPMV_OK;
 }
 
+// sum_csr_duplicates (include/sparse_operation.h:22-73), the compact step of
+// coo_to_csr (include/sparse_conversion.h:82-87): per row, entries of equal
+// column summed; the row's columns come out in the reverse order of their
+// first appearance (the reference chains them head-first) and sums equal to
+// zero are dropped.  In place on host arrays; row_offset is rewritten.
+template <typename V>
+static void sum_duplicates(int64_t m, int64_t n, int32_t *rp, int32_t *ci, V *cv) {
+    std::vector<int32_t> next((size_t)n, -1);
+    std::vector<V> sums((size_t)n, V(0));
+    int64_t nnz = 0, row_end = 0;
+    for (int64_t i = 0; i < m; i++) {
+        int32_t head = -2;
+        const int64_t row_start = row_end;
+        row_end = rp[i + 1];
+        for (int64_t jj = row_start; jj < row_end; jj++) {
+            const int32_t j = ci[jj];
+            sums[(size_t)j] += cv[jj];
+            if (next[(size_t)j] == -1) {
+                next[(size_t)j] = head;
+                head = j;
+            }
+        }
+        while (head != -2) {
+            const int32_t cur = head;
+            head = next[(size_t)cur];
+            if (sums[(size_t)cur] != V(0)) {
+                ci[nnz] = cur;
+                cv[nnz] = sums[(size_t)cur];
+                nnz++;
+            }
+            next[(size_t)cur] = -1;
+            sums[(size_t)cur] = V(0);
+        }
+        rp[i + 1] = (int32_t)nnz;
+    }
+}
+
+extern "C" sspmv_status sspmv_sum_csr_duplicates(int32_t value_type, int64_t num_rows, int64_t num_cols,
+                                                 int32_t *row_offset, int32_t *col_index, void *values,
+                                                 int64_t *num_nnzs) {
+    if (!row_offset || num_rows < 0 || num_cols < 0) return fail(SSPMV_INVALID_ARG, "bad arguments");
+    if (row_offset[num_rows] > 0 && (!col_index || !values)) return fail(SSPMV_INVALID_ARG, "null array");
+    for (int64_t k = 0; k < row_offset[num_rows]; k++)
+        if (col_index[k] < 0 || col_index[k] >= num_cols) return fail(SSPMV_INVALID_ARG, "column out of range");
+    if (value_type == SSPMV_F64) sum_duplicates(num_rows, num_cols, row_offset, col_index, (double *)values);
+    else if (value_type == SSPMV_F32) sum_duplicates(num_rows, num_cols, row_offset, col_index, (float *)values);
+    else return fail(SSPMV_INVALID_ARG, "bad value_type");
+    if (num_nnzs) *num_nnzs = row_offset[num_rows];
+    return SSPMV_OK;
+}
+
 extern "C" sspmv_status sspmv_write_mtx(const char *path, int64_t num_rows, int64_t num_cols,
                                         const int32_t *row_offset, const int32_t *col_index, const double *values) {
     if (!path || !row_offset) return fail(SSPMV_INVALID_ARG, "null argument");

@@ -358,8 +358,22 @@ def fp64_ceiling(stream=None) -> float:
     return rate.value
 
 
-def read_csr_matrix(path: str, precision: int = 64) -> HostCSR:
-    """read_csr_matrix (utils/sparse_io.cpp:180-204) on the host."""
+def sum_csr_duplicates(A: HostCSR) -> HostCSR:
+    """sum_csr_duplicates (include/sparse_operation.h:22-73) on a copy of A:
+    equal columns of a row summed, columns in reverse order of first
+    appearance, zero sums dropped."""
+    rp = np.array(A.row_offset, np.int32)
+    ci = np.array(A.col_index, np.int32)
+    cv = np.array(A.values)
+    nnz = C.c_int64(0)
+    call("sspmv_sum_csr_duplicates", _vt(cv.dtype), A.num_rows, A.num_cols, rp.ctypes.data_as(C.c_void_p),
+         ci.ctypes.data_as(C.c_void_p), cv.ctypes.data_as(C.c_void_p), C.byref(nnz))
+    return HostCSR(A.num_rows, A.num_cols, rp, ci[:nnz.value].copy(), cv[:nnz.value].copy())
+
+
+def read_csr_matrix(path: str, precision: int = 64, compact: bool = False) -> HostCSR:
+    """read_csr_matrix (utils/sparse_io.cpp:180-204) on the host; compact:
+    duplicates summed (sum_csr_duplicates)."""
     vt = F64 if precision == 64 else F32
     m, n, nnz = C.c_int64(), C.c_int64(), C.c_int64()
     call("sspmv_read_mtx", str(path).encode(), vt, C.byref(m), C.byref(n), C.byref(nnz), None, None, None)
@@ -368,7 +382,8 @@ def read_csr_matrix(path: str, precision: int = 64) -> HostCSR:
     val = np.empty(nnz.value, np.float64 if vt == F64 else np.float32)
     call("sspmv_read_mtx", str(path).encode(), vt, C.byref(m), C.byref(n), C.byref(nnz),
          rp.ctypes.data_as(C.c_void_p), col.ctypes.data_as(C.c_void_p), val.ctypes.data_as(C.c_void_p))
-    return HostCSR(int(m.value), int(n.value), rp, col, val)
+    A = HostCSR(int(m.value), int(n.value), rp, col, val)
+    return sum_csr_duplicates(A) if compact else A
 
 
 def read_coo_triplets(path: str, precision: int = 64):

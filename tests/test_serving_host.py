@@ -57,18 +57,3 @@ def test_latency_summary():
     assert abs(s["p50_us"] - 50.0) < 1.0 and s["p99_us"] <= 99.0
     assert s["mean_batch"] == 4.0
 
-
-def test_read_mtx_coo_file_order(tmp_path):
-    """read_coo_matrix order: triplets as they appear in the file, 1-based to
-    0-based, each symmetric off-diagonal entry followed by its mirror."""
-    from sspmv_gb300 import lespmv as L
-    p = tmp_path / "s.mtx"
-    p.write_text("%%MatrixMarket matrix coordinate real symmetric\n% c\n3 3 4\n3 1 2.5\n1 1 1.0\n2 1 -4\n3 3 7\n")
-    m, n, r, c, v = L.read_coo_triplets(str(p))
-    assert (m, n) == (3, 3)
-    assert r.tolist() == [2, 0, 0, 1, 0, 2]
-    assert c.tolist() == [0, 2, 0, 0, 1, 2]
-    assert v.tolist() == [2.5, 2.5, 1.0, -4.0, -4.0, 7.0]
-    A = L.read_csr_matrix(str(p))
-    assert A.row_offset.tolist() == [0, 3, 4, 6]
-    assert A.col_index.tolist() == [2, 0, 1, 0, 0, 2]
