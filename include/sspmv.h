@@ -414,6 +414,23 @@ double sspmv_algorithmic_bytes_sell(const sspmv_s_ell *A, int32_t k, int32_t bet
 double sspmv_algorithmic_bytes_sell_c_sigma(const sspmv_sell_c_sigma *A, int32_t k, int32_t beta_nonzero);
 double sspmv_algorithmic_bytes_sell_c_R(const sspmv_sell_c_R *A, int32_t k, int32_t beta_nonzero);
 
+/* The reference benchmark's bytes per SpMV, bytes_per_spmv
+ * (include/spmv_benchmark.h:26-150), the numerator of the GB/s its benchmark
+ * programs print (src/spmv_benchmark.cpp:68): x charged per nonzero, y twice
+ * per row, padded slots for ELL and the sliced formats (their values at 4
+ * bytes, as the reference counts them), y of occupied rows only for COO.
+ * From the struct fields, except COO, which counts its occupied rows on the
+ * device (synchronous).  -1 on a null or malformed matrix. */
+double sspmv_reference_bytes_csr(const sspmv_csr *A);
+double sspmv_reference_bytes_csr5(const sspmv_csr5 *A);
+double sspmv_reference_bytes_coo(const sspmv_coo *A);
+double sspmv_reference_bytes_dia(const sspmv_dia *A);
+double sspmv_reference_bytes_bsr(const sspmv_bsr *A);
+double sspmv_reference_bytes_ell(const sspmv_ell *A);
+double sspmv_reference_bytes_sell(const sspmv_s_ell *A);
+double sspmv_reference_bytes_sell_c_sigma(const sspmv_sell_c_sigma *A);
+double sspmv_reference_bytes_sell_c_R(const sspmv_sell_c_R *A);
+
 /* ---------------- matrix features ---------------- */
 /* The reference's MTX feature extractor (src/sparse_features.cpp:122-968) on
  * a device CSR matrix: features[0..39] are the 40 values of its .features

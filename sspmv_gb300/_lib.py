@@ -132,6 +132,7 @@ _SIGS = {
     "sspmv_spmm_csr": (_st, [_d, C.POINTER(Csr), _i32, _vp, _i64, _d, _vp, _i64, _vp]),
     "sspmv_LeSpMV_csr_noalloc": (_st, [_d, C.POINTER(Csr), _vp, _d, _vp, _vp]),
     "sspmv_algorithmic_bytes_csr": (_d, [C.POINTER(Csr), _i32, _i32]),
+    "sspmv_reference_bytes_csr": (_d, [C.POINTER(Csr)]),
     "sspmv_read_mtx": (_st, [C.c_char_p, _i32, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64), _vp, _vp, _vp]),
     "sspmv_write_mtx": (_st, [C.c_char_p, _i64, _i64, _vp, _vp, _vp]),
     "sspmv_synth_row_offsets": (_i64, [C.POINTER(SynthParams), C.c_uint64, _vp]),
@@ -155,6 +156,7 @@ def _format_sigs(fmt: str, struct, convert_args, export_args):
         f"sspmv_spmm_{fmt}": (_st, [_d, P, _i32, _vp, _i64, _d, _vp, _i64, _vp]),
         f"sspmv_delete_{fmt}": (_st, [P]),
         f"sspmv_algorithmic_bytes_{fmt}": (_d, [P, _i32, _i32]),
+        f"sspmv_reference_bytes_{fmt}": (_d, [P]),
         f"sspmv_{fmt}_export": (_st, [P, *export_args, _vp]),
     }
     if convert_args is not None:

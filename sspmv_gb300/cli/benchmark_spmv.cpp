@@ -12,7 +12,9 @@
 // Extra GPU options: --chunkwidth, --slicewidth, --alignment (sliced
 // formats), --blockr / --blockc (BSR), --sigma / --omega (CSR5),
 // --kernel=<flag> (kernel_flag), --perf=<file> (default
-// ./performance/mat_perf.txt, as the reference's MAT_PERFORMANCE).
+// ./performance/mat_perf.txt, as the reference's MAT_PERFORMANCE),
+// --bytes=reference|algorithmic (the byte count behind the printed GB/s:
+// the reference's bytes_per_spmv by default).
 //
 // As the reference does, it reads the matrix (Matrix Market), converts CSR
 // to the format (timed: "format_convert", ms), compares the format's SpMV
@@ -84,6 +86,7 @@ void usage(const char *prog) {
     printf("\t --threads   = CPU threads of the CPU build (accepted, no effect on the GPU)\n");
     printf("\t --ld        = ELL layout recorded in the format (0 row-major, 1 column-major)\n");
     printf("\t --format    = csr|coo|ell|sell|sell_c_sigma|sell_c_R|dia|bsr|csr5 (default: from the program name)\n");
+    printf("\t --bytes     = reference (default: the reference's bytes_per_spmv) | algorithmic (no padding, x and y once)\n");
     printf("\t --chunkwidth, --slicewidth, --alignment, --blockr, --blockc, --sigma, --omega, --kernel, --perf\n");
     printf("Note: my_matrix.mtx must be real-valued sparse matrix in the MatrixMarket file format.\n");
 }
@@ -142,7 +145,20 @@ struct FormatMatrix {
         if (fmt == "csr5") return sspmv_LeSpMV_csr5(a, &csr5, x, b, y, nullptr);
         return sspmv_LeSpMV_csr(a, &csr, x, b, y, nullptr);
     }
-    double bytes() {
+    // The reference's bytes_per_spmv (include/spmv_benchmark.h:26-150).
+    double reference_bytes() {
+        if (fmt == "coo") return sspmv_reference_bytes_coo(&coo);
+        if (fmt == "ell") return sspmv_reference_bytes_ell(&ell);
+        if (fmt == "sell") return sspmv_reference_bytes_sell(&sell);
+        if (fmt == "sell_c_sigma") return sspmv_reference_bytes_sell_c_sigma(&scs);
+        if (fmt == "sell_c_R") return sspmv_reference_bytes_sell_c_R(&scr);
+        if (fmt == "dia") return sspmv_reference_bytes_dia(&dia);
+        if (fmt == "bsr") return sspmv_reference_bytes_bsr(&bsr);
+        if (fmt == "csr5") return sspmv_reference_bytes_csr5(&csr5);
+        return sspmv_reference_bytes_csr(&csr);
+    }
+    // Structural bytes without padding, x and y once (sspmv_algorithmic_bytes_<fmt>).
+    double algorithmic_bytes() {
         if (fmt == "coo") return sspmv_algorithmic_bytes_coo(&coo, 1, 0);
         if (fmt == "ell") return sspmv_algorithmic_bytes_ell(&ell, 1, 0);
         if (fmt == "sell") return sspmv_algorithmic_bytes_sell(&sell, 1, 0);
@@ -276,7 +292,10 @@ int run(int argc, char **argv, const std::string &fmt, const char *path, int32_t
     }
     const double msec = total / iters, sec = msec / 1000.0;
     const double gflops = sec == 0 ? 0 : 2.0 * (double)nnz / sec / 1e9;
-    const double gbytes = sec == 0 ? 0 : F.bytes() / sec / 1e9;
+    const char *bytes_model = get_argval(argc, argv, "bytes");
+    const bool algorithmic = bytes_model && strcmp(bytes_model, "algorithmic") == 0;
+    const double nbytes = algorithmic ? F.algorithmic_bytes() : F.reference_bytes();
+    const double gbytes = sec == 0 || nbytes < 0 ? 0 : nbytes / sec / 1e9;
     printf("\tbenchmarking %-20s [%s]: %8.4f ms ( %5.4f GFLOP/s %5.4f GB/s)\n", (fmt + "_gpu").c_str(), "gpu", msec,
            gflops, gbytes);
 

@@ -98,6 +98,13 @@ class Matrix:
     def algorithmic_bytes(self, k: int = 1, beta_nonzero: bool = False) -> float:
         return float(getattr(lib, f"sspmv_algorithmic_bytes_{self.fmt}")(self.ref(), k, int(beta_nonzero)))
 
+    def reference_bytes(self) -> float:
+        """The reference benchmark's bytes_per_spmv (include/spmv_benchmark.h:26-150)."""
+        b = float(getattr(lib, f"sspmv_reference_bytes_{self.fmt}")(self.ref()))
+        if b < 0:
+            raise RuntimeError(f"reference_bytes({self.fmt}): malformed matrix")
+        return b
+
 
 class CSR_Matrix(Matrix):
     fmt = "csr"

@@ -318,3 +318,46 @@ def test_readers_and_coo_to_ell(tmp_path, oracle_lib):
     for k in e2:
         if isinstance(e2[k], np.ndarray):
             assert np.array_equal(e1[k].view(np.uint8), e2[k].view(np.uint8)), k
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
+def test_reference_bytes_model(dt):
+    """sspmv_reference_bytes_<fmt> equals the reference's bytes_per_spmv
+    (include/spmv_benchmark.h:26-150) restated here from each format's
+    exported arrays: per-chunk widths of the sliced formats, occupied rows of
+    an unsorted COO, BSR block counts, the CSR5 tile count."""
+    from sspmv_gb300 import lespmv as L
+    from sspmv_gb300 import synth
+    A = synth.generate(synth.powerlaw(5000, 1.8, 8.0, 300, 0.1), 4, dtype=dt)
+    M = L.csr_from_host(A)
+    sv, si = np.dtype(dt).itemsize, 4
+    m, nnz = A.num_rows, A.nnz
+    lens = np.diff(A.row_offset)
+    assert M.reference_bytes() == 2 * si * m + si * nnz + 2 * sv * nnz + 2 * sv * m
+    # COO from a permuted copy: y charged for occupied rows only
+    rows = np.repeat(np.arange(m, dtype=np.int32), lens)
+    perm = np.random.default_rng(1).permutation(nnz)
+    coo = L.coo_from_host(m, A.num_cols, rows[perm], A.col_index[perm], A.values[perm])
+    occ = int(np.count_nonzero(lens))
+    assert occ < m
+    assert coo.reference_bytes() == 2 * si * nnz + 2 * sv * nnz + 2 * sv * occ
+    ell = L.csr_to_ell(M, L.RowMajor)
+    w = ell.export()["max_row_width"]
+    assert ell.reference_bytes() == si * m * w + sv * m * w + sv * nnz + 2 * sv * m
+    sell = L.csr_to_sell(M, 8, 4)
+    e = sell.export()
+    slots = int(e["row_width"].astype(np.int64).sum()) * 8
+    assert sell.reference_bytes() == si * e["chunk_num"] + 2 * si * slots + sv * nnz + 2 * sv * m
+    for S, C in ((L.csr_to_sell_c_sigma(M, 64, 16, 0), 16), (L.csr_to_sell_c_R(M, 32, 0), 32)):
+        e = S.export()
+        slots = int(e["chunk_len"].astype(np.int64).sum()) * C
+        assert S.reference_bytes() == si * e["validchunkNum"] + si * m + 2 * si * slots + sv * nnz + 2 * sv * m
+    dia = L.csr_to_dia(L.csr_from_host(synth.generate(synth.banded(4000, [-2, 0, 3]), 5)))
+    sv_d = 8
+    assert dia.reference_bytes() == 2 * sv_d * dia.num_nnzs + 2 * sv_d * 4000
+    bsr = L.csr_to_bsr(M, 4, 2)
+    e = bsr.export()
+    assert bsr.reference_bytes() == (2 * si * e["mb"] + si * e["nnzb"] + 2 * sv * e["nnzb"] * 8 + 2 * sv * m)
+    c5 = L.csr_to_csr5(M)
+    e = c5.export()
+    assert c5.reference_bytes() == 2 * si * m + si * nnz + 2 * sv * nnz + 2 * sv * m + si * e["p"] + si
