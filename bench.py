@@ -219,6 +219,10 @@ def run_gpu(args, rank, world):
     for c in cases:
         c.setdefault("tuned", None)
         c["kernel"] = {"kernel_flag": c["M"].kernel_flag}
+        # secondary byte counts: the reference benchmark's bytes_per_spmv and
+        # the CSR algorithmic bytes of the same matrix (format-independent)
+        c["ref_bytes"] = c["M"].reference_bytes()
+        c["csr_bytes"] = c["csr"].algorithmic_bytes(1, False)
     log("tuned")
 
     def one_step(record):
@@ -268,6 +272,8 @@ def run_gpu(args, rank, world):
         total_bytes += c["bytes"] * len(ms)
         per_case.append({"family": c["fam"], "format": c["fmt"], "dtype": c["dt"], "ms": round(avg, 5),
                          "GBps": round(c["bytes"] / avg / 1e6, 1),
+                         "ref_model_GBps": round(c["ref_bytes"] / avg / 1e6, 1),
+                         "csr_equiv_GBps": round(c["csr_bytes"] / avg / 1e6, 1),
                          "GFLOPs": round(2.0 * c["nnz"] / avg / 1e6, 1),
                          "kernel": c["tuned"] or c["kernel"], "max_norm_err": c["max_norm_err"]})
     step_ms = total_ms / args.steps
