@@ -374,7 +374,12 @@ sspmv_status sspmv_csr_to_bsr(const sspmv_csr *csr, int32_t blockDimRow, int32_t
  * allocated): lets a caller bound the fill before converting. */
 sspmv_status sspmv_csr_count_blocks(const sspmv_csr *csr, int32_t blockDimRow, int32_t blockDimCol, int64_t *nnzb,
                                     sspmv_stream_t stream);
-/* LeSpMV_bsr (src/spmv_bsr.cpp:215-233) */
+/* LeSpMV_bsr (src/spmv_bsr.cpp:215-233).  kernel_flag 0 (default): for
+ * SpMV with r a power of two <= 32 and c in {1,2,4,8,16}, the block-stream
+ * kernel (all lanes on blocks, segmented scan per step) when the thread-per-
+ * row kernel would leave more than half its lane slots idle (uneven block
+ * rows), else the thread-per-row kernel; 1: thread-per-row; 2: block-stream
+ * where the shape allows.  SpMM (k > 1) runs thread-per-row. */
 sspmv_status sspmv_LeSpMV_bsr(double alpha, const sspmv_bsr *A, const void *x, double beta, void *y,
                               sspmv_stream_t stream);
 sspmv_status sspmv_spmm_bsr(double alpha, const sspmv_bsr *A, int32_t k, const void *X, int64_t ldx,

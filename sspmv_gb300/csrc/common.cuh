@@ -157,6 +157,15 @@ __device__ __forceinline__ V axpby(V alpha, V sum, V beta, const V *y) {
     return beta == V(0) ? alpha * sum : alpha * sum + beta * *y;
 }
 
+// n / d for n >= 0 and 1 <= d < 2^31, in 32-bit arithmetic whenever n fits
+// (row and nonzero indices always do: they are int32).  A 64-bit division by
+// a run-time divisor is a long instruction sequence that occupies GB300's
+// narrow FP64 pipe (profiled: the pipe busy well beyond a kernel's DFMA and
+// DMUL counts), the pipe FP64 SpMV needs for its FMAs.
+__device__ __forceinline__ int64_t div_nonneg(int64_t n, int d) {
+    return n <= 0x7fffffff ? (int64_t)((unsigned)n / (unsigned)d) : n / d;
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v, unsigned width = 32) {
     for (unsigned o = width / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, width);

@@ -196,11 +196,11 @@ __global__ void c5_transpose(int64_t nnz, int32_t p, int32_t sigma, int32_t omeg
                              const T *__restrict__ in, T *__restrict__ out) {
     const int64_t tile = (int64_t)sigma * omega;
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t t = k / tile;
+        const int64_t t = div_nonneg(k, (int)tile);
         if (t >= p - 1 || tp[t] == tp[t + 1]) {
             out[k] = in[k];
         } else {
-            const int64_t q = k - t * tile, y = q / omega, x = q - y * omega;  // destination (y, x)
+            const int64_t q = k - t * tile, y = div_nonneg(q, omega), x = q - y * omega;  // destination (y, x)
             out[k] = in[t * tile + x * sigma + y];
         }
     }

@@ -58,10 +58,10 @@ __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
     V alpha, V beta, V *__restrict__ y, int64_t ldy, int64_t cap, const int32_t *__restrict__ ovf_id,
     V *__restrict__ ovf_part) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t c = i / C;
+        const int64_t c = div_nonneg(i, C);
         const int r = (int)(i - c * C);
         const int64_t base = ld_stream(chunk_ptr + c);
-        const int64_t wfull = (ld_stream(chunk_ptr + c + 1) - base) / C;
+        const int64_t wfull = div_nonneg(ld_stream(chunk_ptr + c + 1) - base, C);
         const int64_t w = min(wfull, cap);
         const int32_t *cp = col + base + r;
         const V *vp = val + base + r;
@@ -197,10 +197,10 @@ __global__ void sliced_overflow_fixup(int64_t nov, int64_t nshort, const int32_t
 __global__ void stored_row_lengths(int64_t m, int C, const int64_t *__restrict__ chunk_ptr,
                                    const int32_t *__restrict__ col, int32_t *__restrict__ len) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t c = i / C;
+        const int64_t c = div_nonneg(i, C);
         const int r = (int)(i - c * C);
         const int64_t base = chunk_ptr[c];
-        const int64_t w = (chunk_ptr[c + 1] - base) / C;
+        const int64_t w = div_nonneg(chunk_ptr[c + 1] - base, C);
         int64_t lo = 0, hi = w;  // first padding slot in [0, w]
         while (lo < hi) {
             const int64_t mid = (lo + hi) >> 1;
@@ -228,7 +228,7 @@ __global__ void copy_overflow(int64_t nov, int C, int64_t cap, const int32_t *__
     const int64_t o = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (o >= nov) return;
     const int64_t i = ovf_rows[o];
-    const int64_t c = i / C;
+    const int64_t c = div_nonneg(i, C);
     const int r = (int)(i - c * C);
     const int64_t base = chunk_ptr[c] + cap * C + r;
     const int64_t n = (int64_t)ovf_ptr[o + 1] - ovf_ptr[o], dst = ovf_ptr[o];
@@ -580,7 +580,8 @@ __global__ void __launch_bounds__(256) sliced_fill(int64_t m, int32_t C, const i
             if (len >= kFillLong) {
                 s_long[atomicAdd(&s_count, 1)] = i;
             } else {
-                const int64_t base = chunk_ptr[i / C] + i % C;
+                const int64_t ic = div_nonneg(i, C);
+                const int64_t base = chunk_ptr[ic] + (i - ic * C);
                 for (int64_t k = 0; k < len; k++) {
                     col[base + k * C] = ci[s0 + k];
                     val[base + k * C] = cv[s0 + k];
@@ -592,7 +593,8 @@ __global__ void __launch_bounds__(256) sliced_fill(int64_t m, int32_t C, const i
             const int64_t li = s_long[t];
             const int64_t r = reorder ? reorder[li] : li;
             const int64_t s0 = rp[r], len = rp[r + 1] - s0;
-            const int64_t base = chunk_ptr[li / C] + li % C;
+            const int64_t lc = div_nonneg(li, C);
+            const int64_t base = chunk_ptr[lc] + (li - lc * C);
             for (int64_t k = threadIdx.x; k < len; k += blockDim.x) {
                 col[base + k * C] = ci[s0 + k];
                 val[base + k * C] = cv[s0 + k];

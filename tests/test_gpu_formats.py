@@ -361,3 +361,35 @@ def test_reference_bytes_model(dt):
     c5 = L.csr_to_csr5(M)
     e = c5.export()
     assert c5.reference_bytes() == 2 * si * m + si * nnz + 2 * sv * nnz + 2 * sv * m + si * e["p"] + si
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
+def test_bsr_block_stream_shapes(dt, oracle_lib):
+    """BSR SpMV through the block-stream kernel (kernel_flag 2; r a power of
+    two <= 32, c in {1, 2, 4, 8, 16}), the thread-per-row kernel (kernel_flag
+    1, and the shapes the stream kernel does not take) and the default choice: ragged last block row and
+    column, empty block rows, one long block row spanning many warps' worth
+    of blocks; beta = 0 and beta != 0; both within tolerance of the FP64
+    product and run twice with identical bits."""
+    from sspmv_gb300 import lespmv as L
+    from sspmv_gb300 import synth
+    A = synth.generate(synth.powerlaw(3001, 1.6, 6.0, 2999, 0.3), 11, dt)
+    M = L.csr_from_host(A)
+    nnz_row = np.diff(A.row_offset)
+    x = synth.vector(A.num_cols, 0, dt)
+    y0 = synth.vector(A.num_rows, 9, dt)
+    for r, c in ((1, 1), (2, 2), (4, 4), (8, 4), (16, 8), (32, 2), (4, 16), (3, 4), (4, 3)):
+        B = L.csr_to_bsr(M, r, c)
+        for flag in (0, 1, 2):
+            B.set_kernel(flag, 0)
+            for beta in (0.0, BETA):
+                outs = []
+                for _ in range(2):
+                    Y = to_dev(y0)
+                    L.LeSpMV(ALPHA, B, to_dev(x), beta, Y)
+                    outs.append(to_host(Y))
+                assert np.array_equal(outs[0].view(np.uint8), outs[1].view(np.uint8)), (r, c, flag, beta)
+                y64, absum = oracle_lib.spmm_ref(A, x.reshape(-1, 1), ALPHA, beta, y0.reshape(-1, 1))
+                ok, mx, _ = tolerance_ok(outs[0].reshape(-1, 1), y64, absum, nnz_row, dt, ALPHA, beta,
+                                         y0.reshape(-1, 1))
+                assert ok, f"bsr {r}x{c} flag={flag} beta={beta}: max normalised error {mx}"
