@@ -378,8 +378,9 @@ sspmv_status sspmv_csr_count_blocks(const sspmv_csr *csr, int32_t blockDimRow, i
  * SpMV with r a power of two <= 32 and c in {1,2,4,8,16}, the block-stream
  * kernel (all lanes on blocks, segmented scan per step) when the thread-per-
  * row kernel would leave more than half its lane slots idle (uneven block
- * rows), else the thread-per-row kernel; 1: thread-per-row; 2: block-stream
- * where the shape allows.  SpMM (k > 1) runs thread-per-row. */
+ * rows), else the thread-per-row kernel; 1: thread-per-row (the reference's
+ * flag 1, rows in parallel); 2: block-stream where the shape allows (its flag
+ * 2, balanced over blocks).  SpMM (k > 1) runs thread-per-row. */
 sspmv_status sspmv_LeSpMV_bsr(double alpha, const sspmv_bsr *A, const void *x, double beta, void *y,
                               sspmv_stream_t stream);
 sspmv_status sspmv_spmm_bsr(double alpha, const sspmv_bsr *A, int32_t k, const void *X, int64_t ldx,
