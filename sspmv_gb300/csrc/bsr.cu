@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(kBlock) bsr_stream_kernel(
         if (g == G - 1) next = (k + 1 < k1) ? ld_stream(block_row + k + 1) : -1;
         if (valid && next != br) {  // last block of row br
             const int64_t row = ((int64_t)br << lr) + q;
-            if (row < m) y[row] = plain ? s : axpby(alpha, s, beta, y + row);
+            if (row < m) y[row] = row_out(plain, alpha, s, beta, y + row);
         }
         carry_row = __shfl_sync(0xffffffffu, br, (G - 1) << lr);
         carry = __shfl_sync(0xffffffffu, s, ((G - 1) << lr) + q);

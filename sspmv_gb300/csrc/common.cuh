@@ -157,6 +157,16 @@ __device__ __forceinline__ V axpby(V alpha, V sum, V beta, const V *y) {
     return beta == V(0) ? alpha * sum : alpha * sum + beta * *y;
 }
 
+// A finished row's y value where `plain` (alpha == 1 and beta == 0, the
+// reference's "y = sum" case) is known per thread: the sum itself, exactly
+// alpha * sum, without the FP64 multiply.  Writes of short rows are spread
+// over few lanes of many warp instructions, and GB300's narrow FP64 pipe is
+// paid per warp instruction.
+template <typename V>
+__device__ __forceinline__ V row_out(bool plain, V alpha, V sum, V beta, const V *y) {
+    return plain ? sum : axpby(alpha, sum, beta, y);
+}
+
 // n / d for n >= 0 and 1 <= d < 2^31, in 32-bit arithmetic whenever n fits
 // (row and nonzero indices always do: they are int32).  A 64-bit division by
 // a run-time divisor is a long instruction sequence that occupies GB300's

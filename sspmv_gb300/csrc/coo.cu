@@ -327,7 +327,7 @@ __device__ __forceinline__ void coo_load8(const int32_t *__restrict__ ri, const 
 
 // k = 1: four (FP64) or five (FP32) resident CTAs per SM, the best of 3-6
 // measured on uniform, power-law and banded rows.
-template <typename V, int K>
+template <typename V, int K, bool PLAIN = false>
 __global__ void __launch_bounds__(kBlock, K == 1 ? (sizeof(V) == 4 ? 5 : 4) : 1) coo_warp_kernel(
     int64_t nnz, const int32_t *__restrict__ ri, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
@@ -335,6 +335,7 @@ __global__ void __launch_bounds__(kBlock, K == 1 ? (sizeof(V) == 4 ? 5 : 4) : 1)
     V *__restrict__ head_val, int vec, int xvec) {
     constexpr unsigned kFull = 0xffffffffu;
     const int lane = threadIdx.x & 31;
+    constexpr bool plain = PLAIN;  // alpha == 1 and beta == 0: y = sum
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t j0 = w * kWarpChunk;
     if (j0 >= nnz) return;  // warp-uniform
@@ -389,7 +390,7 @@ __global__ void __launch_bounds__(kBlock, K == 1 ? (sizeof(V) == 4 ? 5 : 4) : 1)
                 } else {
                     V *yp = y + (int64_t)r[u] * ldy;
 #pragma unroll
-                    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, seg[q], beta, yp + q);
+                    for (int q = 0; q < K; q++) yp[q] = row_out(plain, alpha, seg[q], beta, yp + q);
                 }
 #pragma unroll
                 for (int q = 0; q < K; q++) seg[q] = V(0);
@@ -432,7 +433,7 @@ __global__ void __launch_bounds__(kBlock, K == 1 ? (sizeof(V) == 4 ? 5 : 4) : 1)
         } else {
             V *yp = y + (int64_t)head_row * ldy;
 #pragma unroll
-            for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
+            for (int q = 0; q < K; q++) yp[q] = row_out(plain, alpha, tot[q], beta, yp + q);
         }
     }
     const bool chunk_end = __any_sync(kFull, any_end);
@@ -556,9 +557,13 @@ sspmv_status coo_pass(const sspmv_coo *A, Plan *p, V alpha, const V *x, int64_t 
     if (warp_kernel) {
         const int vec = ((reinterpret_cast<uintptr_t>(A->row_index) | reinterpret_cast<uintptr_t>(A->col_index) |
                           reinterpret_cast<uintptr_t>(A->values)) & 15) == 0;
-        coo_warp_kernel<V, K><<<grid_for(nt * 32, kBlock), kBlock, 0, cu(s)>>>(
-            nnz, A->row_index, A->col_index, (const V *)A->values, x, ldx, alpha, beta, y, ldy, ints, ints + nt,
-            (V *)p->extra[which * 3 + 1], (V *)p->extra[which * 3 + 2], vec, xrow_vec(x, ldx, sizeof(V), K));
+        auto go = [&](auto kernel) {
+            kernel<<<grid_for(nt * 32, kBlock), kBlock, 0, cu(s)>>>(
+                nnz, A->row_index, A->col_index, (const V *)A->values, x, ldx, alpha, beta, y, ldy, ints, ints + nt,
+                (V *)p->extra[which * 3 + 1], (V *)p->extra[which * 3 + 2], vec, xrow_vec(x, ldx, sizeof(V), K));
+        };
+        if (K == 1 && alpha == V(1) && beta == V(0)) go(coo_warp_kernel<V, K, K == 1>);
+        else go(coo_warp_kernel<V, K>);
         SSPMV_LAUNCH_CHECK();
         if (nt > 1) {
             coo_fixup<V, K><<<grid_for(nt, 256), 256, 0, cu(s)>>>(nt, A->row_index, tile, ints, ints + nt,

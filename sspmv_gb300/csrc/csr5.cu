@@ -226,7 +226,7 @@ __device__ __forceinline__ uint32_t c5_bit(const uint32_t *d, int lane, int i, i
 
 // SIG > 0: sigma known at compile time (16 or 32, descriptors of at most two
 // packets), so a lane's loop over its sigma nonzeros unrolls fully.
-template <typename V, int K, int OMEGA, int SIG>
+template <typename V, int K, int OMEGA, int SIG, bool PLAIN = false>
 __global__ void __launch_bounds__(kBlock) csr5_tile_kernel(C5View A, const V *__restrict__ x, int64_t ldx, V alpha,
                                                          V beta, V *__restrict__ y, int64_t ldy,
                                                          int32_t *__restrict__ carry_row, int32_t *__restrict__ has_end,
@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(kBlock) csr5_tile_kernel(C5View A, const V *__
                     } else {
                         V *yp = y + map_row(rel) * ldy;
 #pragma unroll
-                        for (int q = 0; q < K; q++) yp[q] = axpby(alpha, sum[q], beta, yp + q);
+                        for (int q = 0; q < K; q++) yp[q] = row_out(PLAIN, alpha, sum[q], beta, yp + q);
                     }
                     rel++;
 #pragma unroll
@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(kBlock) csr5_tile_kernel(C5View A, const V *__
         } else {
             V *yp = y + map_row(yoff) * ldy;
 #pragma unroll
-            for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
+            for (int q = 0; q < K; q++) yp[q] = row_out(PLAIN, alpha, tot[q], beta, yp + q);
         }
     }
     if (active && xl == OMEGA - 1) {  // the tile's last run
@@ -387,7 +387,7 @@ __global__ void __launch_bounds__(kBlock) csr5_tile_kernel(C5View A, const V *__
             } else {
                 V *yp = y + r * ldy;
 #pragma unroll
-                for (int q = 0; q < K; q++) yp[q] = axpby(alpha, sum[q], beta, yp + q);
+                for (int q = 0; q < K; q++) yp[q] = row_out(PLAIN, alpha, sum[q], beta, yp + q);
             }
         }
     }
@@ -536,14 +536,22 @@ sspmv_status launch_c5_tiles(const C5View &v, V alpha, const V *x, int64_t ldx, 
     const int sig = (v.np <= 2 && (v.sigma == 16 || v.sigma == 32)) ? v.sigma : 0;
     if constexpr (K == 1) {  // one right-hand side: sigma-specialised kernels
         if (sig == 16) {
-            csr5_tile_kernel<V, K, OMEGA, 16><<<grid, kBlock, 0, cu(s)>>>(v, x, ldx, alpha, beta, y, ldy, cr, he, cv,
-                                                                          hv);
+            if (alpha == V(1) && beta == V(0))
+                csr5_tile_kernel<V, K, OMEGA, 16, true><<<grid, kBlock, 0, cu(s)>>>(v, x, ldx, alpha, beta, y, ldy, cr,
+                                                                                   he, cv, hv);
+            else
+                csr5_tile_kernel<V, K, OMEGA, 16><<<grid, kBlock, 0, cu(s)>>>(v, x, ldx, alpha, beta, y, ldy, cr, he,
+                                                                              cv, hv);
             SSPMV_LAUNCH_CHECK();
             return SSPMV_OK;
         }
         if (sig == 32) {
-            csr5_tile_kernel<V, K, OMEGA, 32><<<grid, kBlock, 0, cu(s)>>>(v, x, ldx, alpha, beta, y, ldy, cr, he, cv,
-                                                                          hv);
+            if (alpha == V(1) && beta == V(0))
+                csr5_tile_kernel<V, K, OMEGA, 32, true><<<grid, kBlock, 0, cu(s)>>>(v, x, ldx, alpha, beta, y, ldy, cr,
+                                                                                   he, cv, hv);
+            else
+                csr5_tile_kernel<V, K, OMEGA, 32><<<grid, kBlock, 0, cu(s)>>>(v, x, ldx, alpha, beta, y, ldy, cr, he,
+                                                                              cv, hv);
             SSPMV_LAUNCH_CHECK();
             return SSPMV_OK;
         }

@@ -254,7 +254,7 @@ __global__ void csr_merge_fixup(int64_t num_tiles, int m, const int32_t *__restr
     }
 }
 
-template <typename V, int K, int VS>
+template <typename V, int K, int VS, bool PLAIN = false>
 __global__ void __launch_bounds__(kBlock) csr_vector_kernel(
     int m, const int32_t *__restrict__ row_offset, const int32_t *__restrict__ col_index,
     const V *__restrict__ values, const V *__restrict__ x, int64_t ldx, int xvec, V alpha, V beta,
@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(kBlock) csr_vector_kernel(
         if (row < m && sub == 0) {
             V *yp = y + row * ldy;
 #pragma unroll
-            for (int r = 0; r < K; r++) yp[r] = axpby(alpha, s[r], beta, yp + r);
+            for (int r = 0; r < K; r++) yp[r] = row_out(PLAIN, alpha, s[r], beta, yp + r);
         }
     }
 }
@@ -339,9 +339,12 @@ sspmv_status launch_vector_vs(const sspmv_csr *A, V alpha, const V *x, int64_t l
     const int64_t m = A->f.num_rows;
     const int64_t warps = (m + (32 / VS) - 1) / (32 / VS);
     const unsigned grid = grid_for(warps * 32, kBlock, (int64_t)num_sms() * 16);
-    csr_vector_kernel<V, K, VS><<<grid, kBlock, 0, cu(s)>>>((int)m, A->row_offset, A->col_index,
-                                                            (const V *)A->values, x, ldx,
-                                                            xrow_vec(x, ldx, sizeof(V), K), alpha, beta, y, ldy);
+    auto go = [&](auto kernel) {
+        kernel<<<grid, kBlock, 0, cu(s)>>>((int)m, A->row_offset, A->col_index, (const V *)A->values, x, ldx,
+                                           xrow_vec(x, ldx, sizeof(V), K), alpha, beta, y, ldy);
+    };
+    if (K == 1 && alpha == V(1) && beta == V(0)) go(csr_vector_kernel<V, K, VS, K == 1>);
+    else go(csr_vector_kernel<V, K, VS>);
     SSPMV_LAUNCH_CHECK();
     return SSPMV_OK;
 }
@@ -589,7 +592,7 @@ __device__ __forceinline__ void stream_chunk_cols(
 // Chunk w (nonzeros 256w ..) of one matrix, run by one warp; `slot` indexes
 // the carry arrays.  Shared by the single-matrix kernel and the batched
 // serving kernel.
-template <typename V, int K>
+template <typename V, int K, bool PLAIN = false>
 __device__ __forceinline__ void stream_chunk_lanes(
     int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
@@ -597,6 +600,7 @@ __device__ __forceinline__ void stream_chunk_lanes(
     int32_t *__restrict__ has_end, V *__restrict__ carry_val, V *__restrict__ head_val, int vec, int xvec) {
     constexpr unsigned kFull = 0xffffffffu;
     const int lane = threadIdx.x & 31;
+    constexpr bool plain = PLAIN;  // alpha == 1 and beta == 0: y = sum
     const int64_t j0 = w * kStreamChunk;
     if (j0 >= nnz) return;  // warp-uniform
     const int64_t j1 = min(j0 + (int64_t)kStreamChunk, nnz);
@@ -633,7 +637,7 @@ __device__ __forceinline__ void stream_chunk_lanes(
         for (int r2 = 0; r2 < r; r2++) {
             V *yp = y + (int64_t)r2 * ldy;
 #pragma unroll
-            for (int q = 0; q < K; q++) yp[q] = axpby(alpha, V(0), beta, yp + q);
+            for (int q = 0; q < K; q++) yp[q] = row_out(plain, alpha, V(0), beta, yp + q);
         }
     }
     int rend = nv > 0 ? __ldg(rp + r + 1) : 0;
@@ -667,14 +671,14 @@ __device__ __forceinline__ void stream_chunk_lanes(
                 } else {
                     V *yp = y + (int64_t)r * ldy;
 #pragma unroll
-                    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, seg[q], beta, yp + q);
+                    for (int q = 0; q < K; q++) yp[q] = row_out(plain, alpha, seg[q], beta, yp + q);
                 }
 #pragma unroll
                 for (int q = 0; q < K; q++) seg[q] = V(0);
                 for (int r2 = r + 1; r2 < m && __ldg(rp + r2 + 1) == e + 1; r2++) {  // empty rows after r
                     V *yp = y + (int64_t)r2 * ldy;
 #pragma unroll
-                    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, V(0), beta, yp + q);
+                    for (int q = 0; q < K; q++) yp[q] = row_out(plain, alpha, V(0), beta, yp + q);
                 }
             }
         }
@@ -714,7 +718,7 @@ __device__ __forceinline__ void stream_chunk_lanes(
         } else {
             V *yp = y + (int64_t)head_row * ldy;
 #pragma unroll
-            for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
+            for (int q = 0; q < K; q++) yp[q] = row_out(plain, alpha, tot[q], beta, yp + q);
         }
     }
     const bool chunk_end = __any_sync(kFull, any_end);
@@ -738,7 +742,7 @@ __device__ __forceinline__ void stream_chunk_lanes(
 // dependent loads on row_offset.  The arithmetic (per-lane sums in nonzero
 // order, the segmented scan, the carry slots) is that of stream_chunk_lanes,
 // so both give the same bits.  sbits: the warp's 33 words of shared memory.
-template <typename V, int K>
+template <typename V, int K, bool PLAIN = false>
 __device__ __forceinline__ void stream_chunk_fast(
     int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy, const int ra,
@@ -747,6 +751,7 @@ __device__ __forceinline__ void stream_chunk_fast(
     uint32_t *__restrict__ sbits) {
     constexpr unsigned kFull = 0xffffffffu;
     const int lane = threadIdx.x & 31;
+    constexpr bool plain = PLAIN;  // alpha == 1 and beta == 0: y = sum
     const int64_t j0 = w * kStreamChunk;
     const int64_t j1 = min(j0 + (int64_t)kStreamChunk, nnz);
     const int64_t e0 = j0 + (int64_t)lane * kStreamPerLane;
@@ -823,7 +828,7 @@ __device__ __forceinline__ void stream_chunk_fast(
                 } else {
                     V *yp = y + (int64_t)r * ldy;
 #pragma unroll
-                    for (int q = 0; q < K; q++) yp[q] = axpby(alpha, seg[q], beta, yp + q);
+                    for (int q = 0; q < K; q++) yp[q] = row_out(plain, alpha, seg[q], beta, yp + q);
                 }
 #pragma unroll
                 for (int q = 0; q < K; q++) seg[q] = V(0);
@@ -866,7 +871,7 @@ __device__ __forceinline__ void stream_chunk_fast(
         } else {
             V *yp = y + (int64_t)head_row * ldy;
 #pragma unroll
-            for (int q = 0; q < K; q++) yp[q] = axpby(alpha, tot[q], beta, yp + q);
+            for (int q = 0; q < K; q++) yp[q] = row_out(plain, alpha, tot[q], beta, yp + q);
         }
     }
     const bool chunk_end = __any_sync(kFull, any_end);
@@ -885,7 +890,7 @@ __device__ __forceinline__ void stream_chunk_fast(
 // column groups (stream_chunk_cols), which read each 64-byte row of X with
 // one coalesced access (measured 1.3-1.4x faster there; slower for FP32 and
 // mixed for k = 4).
-template <typename V, int K>
+template <typename V, int K, bool PLAIN = false>
 __device__ __forceinline__ void stream_chunk(
     int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
@@ -899,22 +904,24 @@ __device__ __forceinline__ void stream_chunk(
         if (no_empty && w * kStreamChunk < nnz) {  // warp-uniform
             const int ra = __ldg(row_start + w);
             const int last = min(__ldg(row_start + w + 1), m - 1) + 1;
-            stream_chunk_fast<V, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, ra, last, w, slot, carry_row,
-                                    has_end, carry_val, head_val, vec, xvec, sbits);
+            stream_chunk_fast<V, K, PLAIN>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, ra, last, w, slot,
+                                           carry_row, has_end, carry_val, head_val, vec, xvec, sbits);
             return;
         }
-        stream_chunk_lanes<V, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, slot, carry_row,
-                                 has_end, carry_val, head_val, vec, xvec);
+        stream_chunk_lanes<V, K, PLAIN>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, slot,
+                                        carry_row, has_end, carry_val, head_val, vec, xvec);
     }
 }
 
 #define SSPMV_STREAM_KERNEL_BODY                                                                          \
     __shared__ uint32_t s_bits[kBlock / 32][33];                                                          \
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;                              \
-    stream_chunk<V, K>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, w, carry_row, has_end, \
-                       carry_val, head_val, vec, xvec, no_empty, s_bits[threadIdx.x >> 5]);
+    stream_chunk<V, K, PLAIN>(m, nnz, rp, ci, cv, x, ldx, alpha, beta, y, ldy, row_start, w, w, carry_row,    \
+                              has_end, carry_val, head_val, vec, xvec, no_empty, s_bits[threadIdx.x >> 5]);
 
-template <typename V, int K>
+// PLAIN: alpha == 1 and beta == 0 (y = sum), instantiated for k = 1: the
+// rows' writes then carry no FP64 multiply.
+template <typename V, int K, bool PLAIN = false>
 __global__ void __launch_bounds__(kBlock) csr_stream_kernel(
     int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
@@ -925,7 +932,7 @@ __global__ void __launch_bounds__(kBlock) csr_stream_kernel(
 
 // The same kernel held to six resident CTAs per SM (at most 42 registers):
 // measured 5-8% faster for FP32 at k = 1; FP64 slows down when squeezed.
-template <typename V, int K>
+template <typename V, int K, bool PLAIN = false>
 __global__ void __launch_bounds__(kBlock, 6) csr_stream_kernel_occ6(
     int m, int64_t nnz, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const V *__restrict__ cv,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy,
@@ -1003,16 +1010,22 @@ sspmv_status launch_stream(const sspmv_csr *A, Plan *p, V alpha, const V *x, int
     const unsigned grid = grid_for(nt * 32, kBlock);
     const int no_empty = p->extra_i[1] == 0 ? 1 : 0;
     const int xvec = xrow_vec(x, ldx, sizeof(V), K);
-    if constexpr (sizeof(V) == 4 && K == 1)
-        csr_stream_kernel_occ6<V, K><<<grid, kBlock, 0, cu(s)>>>(
-            (int)A->f.num_rows, A->f.num_nnzs, A->row_offset, A->col_index, (const V *)A->values, x, ldx, alpha,
-            beta, y, ldy, (const int32_t *)p->extra[0], ints, ints + nt, (V *)p->extra[2], (V *)p->extra[3], vec,
-            xvec, no_empty);
-    else
-        csr_stream_kernel<V, K><<<grid, kBlock, 0, cu(s)>>>(
-            (int)A->f.num_rows, A->f.num_nnzs, A->row_offset, A->col_index, (const V *)A->values, x, ldx, alpha,
-            beta, y, ldy, (const int32_t *)p->extra[0], ints, ints + nt, (V *)p->extra[2], (V *)p->extra[3], vec,
-            xvec, no_empty);
+    auto go = [&](auto kernel) {
+        kernel<<<grid, kBlock, 0, cu(s)>>>((int)A->f.num_rows, A->f.num_nnzs, A->row_offset, A->col_index,
+                                           (const V *)A->values, x, ldx, alpha, beta, y, ldy,
+                                           (const int32_t *)p->extra[0], ints, ints + nt, (V *)p->extra[2],
+                                           (V *)p->extra[3], vec, xvec, no_empty);
+    };
+    const bool plain = alpha == V(1) && beta == V(0);
+    if constexpr (sizeof(V) == 4 && K == 1) {
+        if (plain) go(csr_stream_kernel_occ6<V, K, true>);
+        else go(csr_stream_kernel_occ6<V, K>);
+    } else if constexpr (K == 1) {
+        if (plain) go(csr_stream_kernel<V, K, true>);
+        else go(csr_stream_kernel<V, K>);
+    } else {
+        go(csr_stream_kernel<V, K>);
+    }
     SSPMV_LAUNCH_CHECK();
     if (nt > 1) {
         csr_stream_fixup<V, K><<<grid_for(nt, 256), 256, 0, cu(s)>>>(nt, A->row_offset, ints, ints + nt,
