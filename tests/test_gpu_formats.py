@@ -393,3 +393,29 @@ def test_bsr_block_stream_shapes(dt, oracle_lib):
                 ok, mx, _ = tolerance_ok(outs[0].reshape(-1, 1), y64, absum, nnz_row, dt, ALPHA, beta,
                                          y0.reshape(-1, 1))
                 assert ok, f"bsr {r}x{c} flag={flag} beta={beta}: max normalised error {mx}"
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
+def test_plain_sum_instantiations(dt, oracle_lib):
+    """alpha = 1, beta = 0 (y = sum, the kernels' multiply-free instantiation)
+    through the CSR stream / vector, COO warp, CSR5 tile and BSR kernels, on
+    rows that end at every position of a lane's nonzeros (power-law rows with
+    empty rows): within tolerance of the FP64 product, and y fully written
+    (a NaN-filled y comes back finite)."""
+    from sspmv_gb300 import lespmv as L
+    from sspmv_gb300 import synth
+    A = synth.generate(synth.powerlaw(20000, 1.7, 5.0, 3000, 0.2), 21, dt)
+    M = L.csr_from_host(A)
+    nnz_row = np.diff(A.row_offset)
+    x = synth.vector(A.num_cols, 0, dt)
+    y64, absum = oracle_lib.spmm_ref(A, x.reshape(-1, 1), 1.0, 0.0, None)
+    cases = [("csr0", M, 0), ("csr1", M, 1), ("csr3", M, 3), ("coo", L.csr_to_coo(M), 0),
+             ("csr5", L.csr_to_csr5(M), 0), ("bsr", L.csr_to_bsr(M, 4, 4), 2)]
+    for name, G, flag in cases:
+        G.set_kernel(flag, 0)
+        Y = to_dev(np.full(A.num_rows, np.nan, dt))
+        L.LeSpMV(1.0, G, to_dev(x), 0.0, Y)
+        y = to_host(Y)
+        assert np.isfinite(y).all(), name
+        ok, mx, _ = tolerance_ok(y.reshape(-1, 1), y64, absum, nnz_row, dt, 1.0, 0.0, None)
+        assert ok, f"{name}: max normalised error {mx}"
