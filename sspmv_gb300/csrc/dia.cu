@@ -114,7 +114,7 @@ __global__ void dia_fill(int64_t m, int64_t stride, const int32_t *__restrict__ 
         for (int32_t jj = rp[i]; jj < rp[i + 1]; jj++) data[(int64_t)dmap[m - i + ci[jj]] * stride + i] = cv[jj];
 }
 
-template <typename V, int K>
+template <typename V, int K, bool PLAIN = false>
 __global__ void __launch_bounds__(kBlock) dia_spmv_kernel(int m, int n, int nd, int64_t stride,
                                                         const int64_t *__restrict__ offsets,
                                                         const V *__restrict__ data, const V *__restrict__ x,
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(kBlock) dia_spmv_kernel(int m, int n, int nd, 
         }
         V *yp = y + i * ldy;
 #pragma unroll
-        for (int q = 0; q < K; q++) yp[q] = axpby(alpha, s[q], beta, yp + q);
+        for (int q = 0; q < K; q++) yp[q] = row_out(PLAIN, alpha, s[q], beta, yp + q);
     }
 }
 
@@ -164,9 +164,13 @@ template <typename V, int K>
 sspmv_status launch_dia(const sspmv_dia *A, V alpha, const V *x, int64_t ldx, V beta, V *y, int64_t ldy,
                         sspmv_stream_t s) {
     const unsigned grid = grid_for(A->f.num_rows, kBlock, (int64_t)num_sms() * 16);
-    dia_spmv_kernel<V, K><<<grid, kBlock, 0, cu(s)>>>((int)A->f.num_rows, (int)A->f.num_cols, A->complete_ndiags,
-                                                      A->stride, A->diag_offsets, (const V *)A->diag_data, x, ldx,
-                                                      xrow_vec(x, ldx, sizeof(V), K), alpha, beta, y, ldy);
+    auto go = [&](auto kernel) {
+        kernel<<<grid, kBlock, 0, cu(s)>>>((int)A->f.num_rows, (int)A->f.num_cols, A->complete_ndiags, A->stride,
+                                           A->diag_offsets, (const V *)A->diag_data, x, ldx,
+                                           xrow_vec(x, ldx, sizeof(V), K), alpha, beta, y, ldy);
+    };
+    if (K == 1 && alpha == V(1) && beta == V(0)) go(dia_spmv_kernel<V, K, K == 1>);  // y = sum
+    else go(dia_spmv_kernel<V, K>);
     SSPMV_LAUNCH_CHECK();
     return SSPMV_OK;
 }

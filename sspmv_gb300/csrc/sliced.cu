@@ -51,7 +51,7 @@ constexpr int kBlock = 256;
 // share a long row's chunk (slot-major storage puts them in the same sectors).
 constexpr int kSlots = 4;  // slots of a row whose loads are in flight together
 
-template <typename V, int K>
+template <typename V, int K, bool PLAIN = false>
 __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
     int m, int C, const int64_t *__restrict__ chunk_ptr, const int32_t *__restrict__ reorder,
     const int32_t *__restrict__ col, const V *__restrict__ val, const V *__restrict__ x, int64_t ldx, int xvec,
@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(kBlock) sliced_spmv_kernel(
         const int64_t row = reorder ? (int64_t)ld_stream(reorder + i) : i;
         V *yp = y + row * ldy;
 #pragma unroll
-        for (int q = 0; q < K; q++) yp[q] = axpby(alpha, s[q], beta, yp + q);
+        for (int q = 0; q < K; q++) yp[q] = row_out(PLAIN, alpha, s[q], beta, yp + q);
     }
 }
 
@@ -449,10 +449,14 @@ sspmv_status launch_sliced(const SlicedView &v, Plan *p, V alpha, const V *x, in
     const int64_t nov = p ? p->extra_i[1] : 0;
     const unsigned grid = grid_for(v.m, kBlock, (int64_t)num_sms() * 16);
     const int xvec = xrow_vec(x, ldx, sizeof(V), K);
-    sliced_spmv_kernel<V, K><<<grid, kBlock, 0, cu(s)>>>(
-        (int)v.m, v.C, v.chunk_ptr, v.reorder, v.col, (const V *)v.val, x, ldx, xvec, alpha, beta, y, ldy,
-        nov > 0 ? p->extra_i[2] : kNoCap, nov > 0 ? (const int32_t *)p->extra[8] : nullptr,
-        nov > 0 ? (V *)p->extra[4] : nullptr);
+    auto go = [&](auto kernel) {
+        kernel<<<grid, kBlock, 0, cu(s)>>>(
+            (int)v.m, v.C, v.chunk_ptr, v.reorder, v.col, (const V *)v.val, x, ldx, xvec, alpha, beta, y, ldy,
+            nov > 0 ? p->extra_i[2] : kNoCap, nov > 0 ? (const int32_t *)p->extra[8] : nullptr,
+            nov > 0 ? (V *)p->extra[4] : nullptr);
+    };
+    if (K == 1 && alpha == V(1) && beta == V(0)) go(sliced_spmv_kernel<V, K, K == 1>);  // y = sum
+    else go(sliced_spmv_kernel<V, K>);
     SSPMV_LAUNCH_CHECK();
     if (nov > 0) {
         const int64_t nshort = p->extra_i[4], npieces = p->extra_i[5];

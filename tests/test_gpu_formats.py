@@ -398,7 +398,8 @@ def test_bsr_block_stream_shapes(dt, oracle_lib):
 @pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
 def test_plain_sum_instantiations(dt, oracle_lib):
     """alpha = 1, beta = 0 (y = sum, the kernels' multiply-free instantiation)
-    through the CSR stream / vector, COO warp, CSR5 tile and BSR kernels, on
+    through the CSR stream / vector, COO warp, CSR5 tile, BSR and sliced
+    (S-ELL, SELL-c-sigma, SELL-c-R, with their overflow passes) kernels, on
     rows that end at every position of a lane's nonzeros (power-law rows with
     empty rows): within tolerance of the FP64 product, and y fully written
     (a NaN-filled y comes back finite)."""
@@ -410,7 +411,9 @@ def test_plain_sum_instantiations(dt, oracle_lib):
     x = synth.vector(A.num_cols, 0, dt)
     y64, absum = oracle_lib.spmm_ref(A, x.reshape(-1, 1), 1.0, 0.0, None)
     cases = [("csr0", M, 0), ("csr1", M, 1), ("csr3", M, 3), ("coo", L.csr_to_coo(M), 0),
-             ("csr5", L.csr_to_csr5(M), 0), ("bsr", L.csr_to_bsr(M, 4, 4), 2)]
+             ("csr5", L.csr_to_csr5(M), 0), ("bsr", L.csr_to_bsr(M, 4, 4), 2),
+             ("sell", L.csr_to_sell(M, 4, 0), 0), ("scs", L.csr_to_sell_c_sigma(M, 256, 8, 0), 0),
+             ("scr", L.csr_to_sell_c_R(M, 16, 0), 0)]
     for name, G, flag in cases:
         G.set_kernel(flag, 0)
         Y = to_dev(np.full(A.num_rows, np.nan, dt))
