@@ -95,7 +95,7 @@ __global__ void bsr_fill(int64_t m, int32_t r, int32_t c, const int32_t *__restr
     }
 }
 
-template <typename V, int K, int CB>
+template <typename V, int K, int CB, bool PLAIN = false>
 __global__ void __launch_bounds__(kBlock) bsr_spmv_kernel(int m, int n, int r, int cr,
                                                         const int32_t *__restrict__ row_ptr,
                                                         const int32_t *__restrict__ bcol, const V *__restrict__ data,
@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(kBlock) bsr_spmv_kernel(int m, int n, int r, i
         }
         V *yp = y + i * ldy;
 #pragma unroll
-        for (int t = 0; t < K; t++) yp[t] = axpby(alpha, s[t], beta, yp + t);
+        for (int t = 0; t < K; t++) yp[t] = row_out(PLAIN, alpha, s[t], beta, yp + t);
     }
 }
 
@@ -384,10 +384,14 @@ template <typename V, int K, int CB>
 sspmv_status launch_bsr_c(const sspmv_bsr *A, V alpha, const V *x, int64_t ldx, V beta, V *y, int64_t ldy,
                           sspmv_stream_t s) {
     const unsigned grid = grid_for(A->f.num_rows, kBlock, (int64_t)num_sms() * 16);
-    bsr_spmv_kernel<V, K, CB><<<grid, kBlock, 0, cu(s)>>>((int)A->f.num_rows, (int)A->f.num_cols, (int)A->blockDim_r,
-                                                          (int)A->blockDim_c, A->row_ptr, A->block_colindex,
-                                                          (const V *)A->block_data, x, ldx,
-                                                          xrow_vec(x, ldx, sizeof(V), K), alpha, beta, y, ldy);
+    auto go = [&](auto kernel) {
+        kernel<<<grid, kBlock, 0, cu(s)>>>((int)A->f.num_rows, (int)A->f.num_cols, (int)A->blockDim_r,
+                                           (int)A->blockDim_c, A->row_ptr, A->block_colindex,
+                                           (const V *)A->block_data, x, ldx, xrow_vec(x, ldx, sizeof(V), K), alpha,
+                                           beta, y, ldy);
+    };
+    if (K == 1 && alpha == V(1) && beta == V(0)) go(bsr_spmv_kernel<V, K, CB, K == 1>);  // y = sum
+    else go(bsr_spmv_kernel<V, K, CB>);
     SSPMV_LAUNCH_CHECK();
     return SSPMV_OK;
 }
