@@ -10,11 +10,17 @@ A step is one SpMV (y = A*x, alpha=1, beta=0) of every feasible
               the CSR size)
     precision f64, f32
 value = sum of algorithmic bytes / sum of kernel time (GB/s), device-resident
-inputs, L2 flushed (256 MiB write) before every SpMV and excluded from the
-timing.  e2e = the same through the C ABI with pinned host x copied in and y
-copied out of every SpMV inside the timed region, the copies on their own
-streams overlapping the other matrices' SpMVs (serial_value: copies and SpMV
-back to back on one stream).
+inputs, L2 flushed before every SpMV (a 256 MiB write, then a 256 MiB read so
+that no dirty line of the flush is left for the SpMV to write back) and the
+flush excluded from the timing.  e2e = the same through the C ABI with pinned
+host x copied in and y copied out of every SpMV inside the timed region, the
+copies on their own streams overlapping the other matrices' SpMVs
+(serial_value: copies and SpMV back to back on one stream).
+
+The last line on stdout is the compact result (one JSON object of a few KB);
+everything else -- per-format table, sweep points, tuning tables -- goes to
+the detail file (--detail, default gpurun_out/bench_detail.json) and to
+stderr.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl sspmv|reference]
 """
@@ -42,7 +48,7 @@ L2_FLUSH_BYTES = 256 << 20
 RANDOM_COLUMN_FAMILIES = ("uniform_4M", "powerlaw_4M")
 
 
-def parse_args():
+def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -60,7 +66,9 @@ def parse_args():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-large", action="store_true", help="skip the power-law 16M SELL-c-sigma vs CSR section")
     ap.add_argument("--no-serving", action="store_true", help="skip the request-server section")
-    return ap.parse_args()
+    ap.add_argument("--detail", default=str(ROOT / "gpurun_out" / "bench_detail.json"),
+                    help="file for the full result (per-format table, sweeps); '' to skip")
+    return ap.parse_args(argv)
 
 
 _T0 = time.perf_counter()
@@ -73,6 +81,10 @@ def log(msg: str) -> None:
 
 def np_dtype(tag):
     return np.float64 if tag == "f64" else np.float32
+
+
+L2_NOTE = ("flushed before every SpMV (256 MiB write, then 256 MiB read: no dirty flush lines left), "
+           "flush not timed")
 
 
 def scaled_params(name, scale):
@@ -184,7 +196,8 @@ def run_gpu(args, rank, world):
                 cases.append({"fam": fam, "fmt": fmt, "dt": dt, "M": M, "x": x, "y": y,
                               "bytes": M.algorithmic_bytes(1, False), "csr": csr, "nnz": A.nnz,
                               "rows": A.num_rows, "cols": A.num_cols})
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    from sspmv_gb300.autotune import L2Flush
+    flush = L2Flush(dev)
     stream = torch.cuda.current_stream()
     pinned = {}
     if args.csr_kernel:
@@ -227,7 +240,7 @@ def run_gpu(args, rank, world):
 
     def one_step(record):
         for c in cases:
-            flush.zero_()
+            flush()
             e0, e1 = record(c)
             e0.record(stream)
             L.LeSpMV(1.0, c["M"], c["x"], 0.0, c["y"], stream)
@@ -275,7 +288,8 @@ def run_gpu(args, rank, world):
                          "ref_model_GBps": round(c["ref_bytes"] / avg / 1e6, 1),
                          "csr_equiv_GBps": round(c["csr_bytes"] / avg / 1e6, 1),
                          "GFLOPs": round(2.0 * c["nnz"] / avg / 1e6, 1),
-                         "kernel": c["tuned"] or c["kernel"], "max_norm_err": c["max_norm_err"]})
+                         "kernel": c["tuned"] or c["kernel"], "max_norm_err": c["max_norm_err"],
+                         "median_norm_err": c["median_norm_err"]})
     step_ms = total_ms / args.steps
     step_ms = _max_over_ranks(step_ms, world)
     value = total_bytes / args.steps * world / (step_ms * 1e6)
@@ -351,7 +365,7 @@ def run_gpu(args, rank, world):
         "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64+f32", "data": "synthetic (seeded generator, families of the SpMV suite)",
         "config": {"workload": "spmv-suite: " + "+".join(families) + " x " + "+".join(fmts) + " x " + "+".join(dtypes),
-                   "l2": "flushed before every SpMV (256 MiB write), flush not timed",
+                   "l2": L2_NOTE,
                    "alpha": 1.0, "beta": 0.0, "k_rhs": 1, "index": "int32", "parallelism": f"replicas{world}",
                    "skipped": skipped, "scale": args.scale},
         "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches),
@@ -406,7 +420,7 @@ def run_e2e(args, cases, flush, stream, world):
     def serial():
         pairs = []
         for i, c in enumerate(cases):
-            flush.zero_()
+            flush()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             c["x"].copy_(hx[i], non_blocking=True)
@@ -437,10 +451,12 @@ def run_e2e(args, cases, flush, stream, world):
 def check_cases(cases, hosts):
     """Every timed matrix's last y (= A x) on sampled rows -- every 61st row
     and the 64 longest -- against an FP64 product on the same inputs, in units
-    of the per-row bound 8 nnz_i eps sum_j |a_ij x_j| (eps of the value type)."""
+    of the per-row bound 8 nnz_i eps sum_j |a_ij x_j| (eps of the value type).
+    Sets each case's max_norm_err / median_norm_err and returns the summary:
+    max and median per format x precision over the four families."""
     import scipy.sparse as sp
     refs = {}
-    worst = 0.0
+    per = {}
     for c in cases:
         key = (c["fam"], c["dt"])
         if key not in refs:
@@ -457,11 +473,21 @@ def check_cases(cases, hosts):
             refs[key] = (rows, Asp @ x64, bound)
         rows, y64, bound = refs[key]
         yg = c["y"].cpu().numpy()[rows].astype(np.float64)
-        c["max_norm_err"] = round(float((np.abs(yg - y64) / bound).max(initial=0.0)), 4)
-        worst = max(worst, c["max_norm_err"])
+        err = np.abs(yg - y64) / bound
+        c["max_norm_err"] = round(float(err.max(initial=0.0)), 4)
+        c["median_norm_err"] = round(float(np.median(err)) if err.size else 0.0, 5)
+        per.setdefault(f"{c['fmt']}/{c['dt']}", []).append(err)
+    by_fmt = {}
+    worst = 0.0
+    for k, errs in per.items():
+        e = np.concatenate(errs)
+        mx = float(e.max(initial=0.0))
+        worst = max(worst, mx)
+        by_fmt[k] = [round(mx, 4), round(float(np.median(e)), 5)]
     return {"cases": len(cases), "rows": "every 61st and the 64 longest of each matrix",
-            "max_norm_err": worst, "within_tolerance": bool(worst <= 1.0),
-            "tolerance": "|y - y_fp64| <= 8 nnz_i eps sum_j |a_ij x_j| per row"}
+            "max_norm_err": round(worst, 4), "within_tolerance": bool(worst <= 1.0),
+            "tolerance": "|y - y_fp64| <= 8 nnz_i eps sum_j |a_ij x_j| per row",
+            "max_median_by_format": by_fmt}
 
 
 # ------------------------------------------------ large power-law section --
@@ -497,7 +523,8 @@ def run_large(dev, peak):
     n, m = A.num_cols, A.num_rows
     x1 = torch.from_numpy(synth.vector(n, 0, np.float32)).to(dev)
     y1 = torch.zeros(m, dtype=torch.float32, device=dev)
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    from sspmv_gb300.autotune import L2Flush
+    flush = L2Flush(dev)
     out = {"workload": "powerlaw_16M f32 (Zipf 2.0, mean 16, cap 50k)", "num_rows": m, "nnz": A.nnz, "formats": {}}
     res_csr = autotune.tune_format(csr, x1, y1)
     sig_n = -(-m // 32) * 32
@@ -526,7 +553,7 @@ def run_large(dev, peak):
             Y = torch.zeros((m, k), dtype=torch.float32, device=dev)
             ts = []
             for i in range(6):
-                flush.zero_()
+                flush()
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 e0.record()
                 L.spmm(1.0, M, X, 0.0, Y)
@@ -574,7 +601,7 @@ def run_laplacian(dev, peak):
     x = torch.from_numpy(synth.vector(A.num_cols, 0)).to(dev)
     y = torch.zeros(A.num_rows, dtype=torch.float64, device=dev)
     tuned = autotune.tune_format(csr, x, y)
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    flush = autotune.L2Flush(dev)
     cold = autotune.time_spmv(csr, x, y, reps=50, warmup=5, flush=flush)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     for _ in range(5):
@@ -620,13 +647,19 @@ def cpu_sample(A, frac=0.125):
     return HostCSR(r, A.num_cols, A.row_offset[:r + 1].copy(), A.col_index[:nnz], A.values[:nnz])
 
 
+# The reference's CSR5 SpMV (src/spmv_csr5.cpp) is written with x86 AVX-512
+# intrinsics that only ICC accepts: it has no CPU implementation to time on
+# the GB300's Arm host, so the CPU legs leave CSR5 out and say so.
+CPU_UNAVAILABLE = {"csr5": "unavailable on aarch64 host (reference CSR5 SpMV is x86 AVX-512 only)"}
+
+
 def _cpu_convert(O, fmt, A):
     """Oracle (CPU restatement) conversion of a sample for the CPU timing; None if infeasible."""
-    from sspmv_gb300.lespmv import feasible_host
+    from sspmv_gb300.formats import feasible_host
     ok, _ = feasible_host(fmt, A)
-    if not ok:
+    if not ok or fmt in CPU_UNAVAILABLE:
         return None
-    if fmt == "csr" or fmt == "csr5":
+    if fmt == "csr":
         return {}
     if fmt == "coo":
         return O.csr_to_coo(A)
@@ -649,7 +682,7 @@ def _cpu_convert(O, fmt, A):
     if fmt == "dia":
         return O.csr_to_dia(A)
     if fmt == "bsr":
-        from sspmv_gb300.lespmv import bsr_block_for
+        from sspmv_gb300.formats import bsr_block_for
         r, c = bsr_block_for(A)
         return O.csr_to_bsr(A, r, c)
     return None
@@ -658,7 +691,7 @@ def _cpu_convert(O, fmt, A):
 def _cpu_bytes(fmt, A, d, sv):
     m, n, nnz = A.num_rows, A.num_cols, A.nnz
     xb, yb = n * sv, m * sv
-    if fmt in ("csr", "csr5"):
+    if fmt == "csr":
         return nnz * (sv + 4) + (m + 1) * 4 + xb + yb
     if fmt == "coo":
         return nnz * (sv + 8) + xb + yb
@@ -675,7 +708,10 @@ def _cpu_bytes(fmt, A, d, sv):
 
 def cpu_sweep(hosts, families, dtypes, fmts, budget_s, frac=0.125):
     """Times the oracle port's OpenMP SpMV kernels (all host threads) on the
-    first `frac` of the rows of every matrix.  Returns (GB/s, seconds, threads)."""
+    first `frac` of the rows of every matrix.  The oracle restates the
+    reference's OpenMP kernels (src/spmv_<fmt>.cpp); the reference's own
+    sources are not present where the benchmark runs.  Returns (GB/s,
+    seconds, threads, sweeps)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     from oracle import Oracle
     O = Oracle()
@@ -696,9 +732,8 @@ def cpu_sweep(hosts, families, dtypes, fmts, budget_s, frac=0.125):
     reps = 0
     while True:
         for fmt, A, d, x, y, b in prepared:
-            fmt_o = "csr" if fmt == "csr5" else fmt
             t0 = time.perf_counter()
-            O.spmv(fmt_o, d, A, 1.0, x, 0.0, y)
+            O.spmv(fmt, d, A, 1.0, x, 0.0, y)
             tot_t += time.perf_counter() - t0
             tot_b += b
         reps += 1
@@ -711,7 +746,7 @@ def cpu_baseline(hosts, families, dtypes, fmts, budget_s):
     gbs, secs, threads, reps = cpu_sweep(hosts, families, dtypes, fmts, budget_s)
     return {"value": round(gbs, 2), "unit": "GB/s", "cores": threads, "kind": "port",
             "sample": f"first 1/8 of the rows of every matrix, {reps} sweep(s), {secs:.1f} s of SpMV time; "
-                      "oracle restatement of the reference's OpenMP kernels (csr5 timed as csr)"}
+                      "oracle restatement of the reference's OpenMP kernels; csr5 " + CPU_UNAVAILABLE["csr5"]}
 
 
 def run_reference(args, rank, world):
@@ -719,8 +754,8 @@ def run_reference(args, rank, world):
         return None
     families = [f for f in args.families.split(",") if f]
     dtypes = [d for d in args.dtypes.split(",") if d]
-    from sspmv_gb300 import lespmv as L
-    fmts = L.FORMATS if args.formats == "all" else args.formats.split(",")
+    from sspmv_gb300.formats import FORMATS
+    fmts = FORMATS if args.formats == "all" else args.formats.split(",")
     hosts = host_matrices(families, args.scale)
     for _ in range(args.warmup):
         cpu_sweep(hosts, families, dtypes, fmts, budget_s=0.0)
@@ -739,7 +774,8 @@ def run_reference(args, rank, world):
             "config": {"workload": "spmv-suite: " + "+".join(families) + " x " + "+".join(fmts) + " x " + "+".join(dtypes),
                        "sample": "first 1/8 of the rows of every matrix", "wall_s": round(time.perf_counter() - t0, 2)},
             "cpu_baseline": {"value": round(gbs, 2), "unit": "GB/s", "cores": threads, "kind": "port",
-                             "sample": "first 1/8 of the rows of every matrix, one sweep per step"},
+                             "sample": "first 1/8 of the rows of every matrix, one sweep per step; csr5 "
+                                       + CPU_UNAVAILABLE["csr5"]},
             "e2e": {"value": round(gbs, 2), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -769,6 +805,98 @@ def _max_over_ranks(v, world):
     return float(t.item())
 
 
+# ------------------------------------------------------------- output ----
+HEADLINE_LIMIT = 4000
+
+
+def _by_format_GBps(per_case):
+    """Algorithmic bytes / kernel time per format x precision over the four
+    families (sum of bytes / sum of time)."""
+    acc = {}
+    for pc in per_case:
+        k = f"{pc['format']}/{pc['dtype']}"
+        b, t = acc.get(k, (0.0, 0.0))
+        acc[k] = (b + pc["GBps"] * pc["ms"], t + pc["ms"])
+    return {k: round(b / t, 1) for k, (b, t) in acc.items() if t > 0}
+
+
+def headline(out: dict) -> dict:
+    """The compact result line: the contract keys, the roofline and CPU
+    baseline, parity max / median per format x precision, and one-number
+    summaries of the Laplacian, 16M power-law and serving sections (their
+    full records are in the detail file)."""
+    h = {k: out[k] for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+                             "higher_is_better", "scaling", "vs_baseline", "dtype", "data") if k in out}
+    cfg = dict(out.get("config", {}))
+    skipped = cfg.pop("skipped", [])
+    cfg["skipped"] = len(skipped)
+    h["config"] = cfg
+    e2e = out.get("e2e")
+    if e2e:
+        h["e2e"] = {k: e2e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step",
+                                        "ms_per_step", "serial_value") if k in e2e}
+    rf = out.get("roofline")
+    if rf:
+        h["roofline"] = {k: rf.get(k) for k in ("bound", "achieved", "peak", "unit", "frac", "traffic", "kernel",
+                                                "algorithmic_bytes", "peak_kind")}
+        for extra in ("gather_ceiling", "fp64_ceiling"):
+            if rf.get(extra):
+                h["roofline"][extra + "_frac"] = rf[extra]["frac"]
+    h["cpu_baseline"] = out.get("cpu_baseline")
+    h["clocks"] = out.get("clocks")
+    h["gpu_launches"] = out.get("gpu_launches")
+    par = out.get("parity") or {}
+    h["parity"] = {"within_tolerance": par.get("within_tolerance"), "max_norm_err": par.get("max_norm_err"),
+                   "max_median_by_format": par.get("max_median_by_format"), "tolerance": par.get("tolerance")}
+    if out.get("per_format"):
+        h["GBps_by_format"] = _by_format_GBps(out["per_format"])
+    lap = out.get("laplacian_1024")
+    if lap:
+        h["laplacian_1024"] = {k: lap.get(k) for k in ("cold_GBps", "cold_frac_of_measured_peak", "cold_ms",
+                                                       "warm_GBps", "max_norm_err", "median_norm_err")}
+        h["laplacian_1024"]["kernel"] = (lap.get("kernel") or {}).get("kernel_flag"), (lap.get("kernel") or {}).get("param")
+    large = out.get("large_powerlaw_16M")
+    if large:
+        h["large_powerlaw_16M"] = {f"{f}_k{k}_GBps": large["formats"][f][f"k{k}"]["GBps"]
+                                   for f in large.get("formats", {}) for k in (1, 8)}
+        h["large_powerlaw_16M"]["max_norm_err"] = max(large["formats"][f][f"k{k}"]["max_norm_err"]
+                                                      for f in large["formats"] for k in (1, 8))
+    srv = out.get("serving")
+    if srv:
+        h["serving"] = {}
+        for kind in ("host", "device"):
+            r = srv.get(kind)
+            if not r:
+                continue
+            h["serving"][kind] = {"saturation_ratio": {m: round(v, 3) for m, v in r.get("saturation_ratio", {}).items()},
+                                  "equal_p99_ratio": {m: (round(v["throughput_ratio"], 3)
+                                                          if v.get("throughput_ratio") is not None else None)
+                                                      for m, v in r.get("equal_p99", {}).items()}}
+    line = json.dumps(h, separators=(",", ":"))
+    # stay within the limit: drop the least important summaries first
+    for key in ("serving", "large_powerlaw_16M", "GBps_by_format"):
+        if len(line) <= HEADLINE_LIMIT:
+            break
+        h.pop(key, None)
+        line = json.dumps(h, separators=(",", ":"))
+    return h
+
+
+def emit(out: dict, args) -> None:
+    """Full record to the detail file, compact line as the last stdout line."""
+    if args.detail:
+        try:
+            Path(args.detail).parent.mkdir(parents=True, exist_ok=True)
+            Path(args.detail).write_text(json.dumps(out, indent=1))
+            log(f"detail written to {args.detail}")
+        except OSError as e:
+            log(f"detail not written: {e}")
+    h = headline(out)
+    if args.detail:
+        h["detail"] = str(Path(args.detail).relative_to(ROOT)) if Path(args.detail).is_relative_to(ROOT) else args.detail
+    print(json.dumps(h, separators=(",", ":")), flush=True)
+
+
 def main():
     args = parse_args()
     rank, world = _dist()
@@ -784,7 +912,7 @@ def main():
         dist.init_process_group("nccl")
     out = run_gpu(args, rank, world)
     if rank == 0:
-        print(json.dumps(out))
+        emit(out, args)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

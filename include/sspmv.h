@@ -224,11 +224,19 @@ sspmv_status sspmv_gather_ceiling(int32_t value_type, int64_t num_cols, int64_t 
 sspmv_status sspmv_fp64_ceiling(double *fmas_per_second, sspmv_stream_t stream);
 /* Selects the SpMV kernel of a matrix (pass &A->f): kernel_flag as in each
  * format's LeSpMV entry, param a kernel parameter (0 lets the library
- * choose): CSR vector kernel: lanes per row 2..32; S-ELL, SELL-c-sigma,
+ * choose): CSR vector kernel: lanes per row 2..32; CSR row-block kernel:
+ * nonzeros per block window (512, 1024, 2048, 4096); S-ELL, SELL-c-sigma,
  * SELL-c-R: the slots a row's thread reads before the rest of the row moves
  * to the overflow CSR pass (default: a cost model over the row lengths).
  * Used by the autotuner. */
 sspmv_status sspmv_set_kernel(sspmv_features *f, int32_t kernel_flag, int32_t param);
+
+/* Number of bounded device-side waits (a kernel waiting for its own bulk
+ * copies into shared memory) that gave up since the library was loaded, on
+ * the current device.  A wait that gives up leaves its kernel's output
+ * incomplete; 0 in every correct run.  No reference counterpart (the
+ * reference has no device code).  Synchronizes the device. */
+sspmv_status sspmv_wait_timeouts(int64_t *count);
 
 /* ---------------- CSR creation ---------------- */
 /* Device CSR from arrays.  from_host != 0: copies host arrays to library-
@@ -246,10 +254,13 @@ sspmv_status sspmv_csr_export(const sspmv_csr *A, int32_t *row_offset, int32_t *
 sspmv_status sspmv_delete_csr(sspmv_csr *A);
 
 /* ---------------- SpMV / SpMM ---------------- */
-/* LeSpMV_csr (src/spmv_csr.cpp:165-185).  kernel_flag 0 (default) / 3:
+/* LeSpMV_csr (src/spmv_csr.cpp:165-185).  kernel_flag 0 (default):
  * nonzero-split stream kernel (256 nonzeros per warp; matrices with runs of
  * more than 256 empty rows use merge-path); 2: nnz-balanced merge-path
- * kernel; 1: vector-per-row kernel (param: lanes per row). */
+ * kernel; 1: vector-per-row kernel (param: lanes per row); 3: row-block
+ * kernel for matrices whose rows all have at most 64 nonzeros (one CTA per
+ * block of whole rows, param: nonzeros per block window, 512..4096; one
+ * right-hand side; other matrices and k > 1 run the default kernel). */
 sspmv_status sspmv_LeSpMV_csr(double alpha, const sspmv_csr *A, const void *x, double beta, void *y,
                               sspmv_stream_t stream);
 sspmv_status sspmv_spmm_csr(double alpha, const sspmv_csr *A, int32_t k, const void *X, int64_t ldx,

@@ -93,12 +93,7 @@ class Csr5(C.Structure):
                 ("tile_desc_offset_ptr", P32), ("tile_desc_offset", P32)]
 
 
-class SynthParams(C.Structure):
-    _fields_ = [("family", C.c_int32), ("num_offsets", C.c_int32), ("num_rows", C.c_int64),
-                ("num_cols", C.c_int64), ("grid", C.c_int64), ("offsets", C.c_int64 * 32),
-                ("alpha", C.c_double), ("mean", C.c_double), ("cap", C.c_int64),
-                ("block_dim", C.c_int64), ("num_blocks", C.c_int64), ("per_row", C.c_int64),
-                ("empty_row_frac", C.c_double)]
+from .synth import SynthParams  # noqa: E402  (argument type of the sspmv_synth_* exports)
 
 
 def _load():
@@ -131,6 +126,7 @@ _SIGS = {
     "sspmv_LeSpMV_csr": (_st, [_d, C.POINTER(Csr), _vp, _d, _vp, _vp]),
     "sspmv_spmm_csr": (_st, [_d, C.POINTER(Csr), _i32, _vp, _i64, _d, _vp, _i64, _vp]),
     "sspmv_LeSpMV_csr_noalloc": (_st, [_d, C.POINTER(Csr), _vp, _d, _vp, _vp]),
+    "sspmv_wait_timeouts": (_st, [C.POINTER(_i64)]),
     "sspmv_algorithmic_bytes_csr": (_d, [C.POINTER(Csr), _i32, _i32]),
     "sspmv_reference_bytes_csr": (_d, [C.POINTER(Csr)]),
     "sspmv_read_mtx": (_st, [C.c_char_p, _i32, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64), _vp, _vp, _vp]),

@@ -6,7 +6,9 @@ on the GPU, timed with CUDA events with L2 flushed before every run, and the
 fastest is kept.  Results are plain dicts, so a caller can store them as an
 append-only JSONL log keyed by matrix and re-apply them without re-measuring.
 
-CSR candidates: stream kernel (default), merge-path kernel, vector kernel with 2..32 lanes per row.
+CSR candidates: stream kernel (default), merge-path kernel, vector kernel with
+2..32 lanes per row, row-block kernel (short rows) with windows of 512..4096
+nonzeros.
 S-ELL / SELL-c-sigma / SELL-c-R: after the layout, the thread-pass cap (the
 cost model's choice against caps of 16..128 slots).
 SELL-c-sigma candidates (re-conversion per point): C in {8,16,32} x sigma in
@@ -22,15 +24,34 @@ from . import lespmv as L
 L2_FLUSH = 256 << 20
 
 
+class L2Flush:
+    """Evicts the 129 MB L2 between timed SpMVs: a 256 MiB write, then a
+    256 MiB read.  The read pass leaves only clean lines, so the timed kernel
+    does not pay for writing the flush's dirty lines back to HBM (about 5 us
+    on an 84 MB matrix, a quarter of its SpMV).  Call it on the stream the
+    timed kernel runs on (the current stream)."""
+
+    def __init__(self, device):
+        import torch
+        self.w = torch.empty(L2_FLUSH // 4, dtype=torch.float32, device=device)
+        self.r = torch.zeros(L2_FLUSH // 4, dtype=torch.float32, device=device)
+        self.acc = torch.zeros((), dtype=torch.float32, device=device)
+
+    def __call__(self):
+        import torch
+        self.w.zero_()
+        torch.sum(self.r, dim=0, out=self.acc)
+
+
 def time_spmv(M, x, y, reps: int = 10, warmup: int = 2, flush=None, stream=None) -> float:
     """Median milliseconds of one SpMV (alpha=1, beta=0) with L2 flushed."""
     import torch
     stream = stream or torch.cuda.current_stream()
     if flush is None:
-        flush = torch.empty(L2_FLUSH // 4, dtype=torch.float32, device=x.device)
+        flush = L2Flush(x.device)
     ts = []
     for i in range(warmup + reps):
-        flush.zero_()
+        flush()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         L.LeSpMV(1.0, M, x, 0.0, y, stream)
@@ -42,13 +63,13 @@ def time_spmv(M, x, y, reps: int = 10, warmup: int = 2, flush=None, stream=None)
     return ts[len(ts) // 2]
 
 
-CSR_CANDIDATES = [(0, 0), (2, 0)] + [(1, vs) for vs in (2, 4, 8, 16, 32)]
+CSR_CANDIDATES = ([(0, 0), (2, 0)] + [(1, vs) for vs in (2, 4, 8, 16, 32)] +
+                  [(3, w) for w in (512, 1024, 2048, 4096)])
 
 
 def tune_kernel(M, x, y, candidates, reps: int = 10) -> dict:
     """Times each (kernel_flag, param) on matrix M, applies the fastest."""
-    import torch
-    flush = torch.empty(L2_FLUSH // 4, dtype=torch.float32, device=x.device)
+    flush = L2Flush(x.device)
     table = []
     for flag, param in candidates:
         M.set_kernel(flag, param)
@@ -96,8 +117,7 @@ def tune_conversion(csr, fmt: str, x, y, reps: int = 8, max_fill: float = 4.0):
     """Converts `csr` with each candidate parameter set of `fmt`, times one
     SpMV of each and keeps the fastest.  Returns (matrix, record) or
     (None, None) when no candidate converts."""
-    import torch
-    flush = torch.empty(L2_FLUSH // 4, dtype=torch.float32, device=x.device)
+    flush = L2Flush(x.device)
     best, table = None, []
     for kw in conversion_candidates(fmt, csr.num_rows):
         if fmt == "bsr":
@@ -159,7 +179,7 @@ def kernel_table(families, dtypes=("f64", "f32"), ks=(1, 2, 4, 8), flags=((0, 0)
     import numpy as np
     import torch
     from . import synth
-    flush = torch.empty(L2_FLUSH // 4, dtype=torch.float32, device="cuda")
+    flush = L2Flush("cuda")
     out = []
     for fam in families:
         for dt in dtypes:
@@ -173,7 +193,7 @@ def kernel_table(families, dtypes=("f64", "f32"), ks=(1, 2, 4, 8), flags=((0, 0)
                     csr.set_kernel(flag, param)
                     ts = []
                     for i in range(reps + 1):
-                        flush.zero_()
+                        flush()
                         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                         e0.record()
                         L.spmm(1.0, csr, X, 0.0, Y)

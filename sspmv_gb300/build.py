@@ -77,6 +77,26 @@ def build_library(verbose: bool = False, extra: list[str] | None = None, jobs: i
     return LIB
 
 
+SYNTH_LIB = LIBDIR / "libsspmv_synth.so"
+
+
+def build_synth() -> Path:
+    """lib/libsspmv_synth.so: the seeded matrix generator (csrc/synth.cpp)
+    alone, host code only, so CPU-only callers need not load libsspmv.so."""
+    LIBDIR.mkdir(exist_ok=True)
+    src = CSRC / "synth.cpp"
+    hdr = ROOT / "include" / "sspmv.h"
+    if SYNTH_LIB.exists() and SYNTH_LIB.stat().st_mtime >= max(src.stat().st_mtime, hdr.stat().st_mtime):
+        return SYNTH_LIB
+    cxx = os.environ.get("CXX", "g++")
+    cmd = [cxx, "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-shared", f"-I{ROOT / 'include'}", str(src),
+           "-o", str(SYNTH_LIB)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"synth build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return SYNTH_LIB
+
+
 CLI_SRC = PKG / "cli" / "benchmark_spmv.cpp"
 BINDIR = PKG / "bin"
 CLI_FORMATS = ("csr", "coo", "ell", "sell", "sell_c_sigma", "sell_c_R", "dia", "bsr", "csr5")
@@ -116,5 +136,6 @@ def build_oracle(with_reference: bool | None = None) -> None:
 
 if __name__ == "__main__":
     print(build_library(verbose=True))
+    print(build_synth())
     print(build_cli())
     build_oracle()

@@ -3,9 +3,10 @@
 // Replaces LeSpMV_csr (src/spmv_csr.cpp:165-185) and its three CPU kernels
 // (serial, OpenMP per row, nnz-balanced row partition).
 //
-// Default kernel (kernel_flag 0 or 3): the nonzero-split stream kernel (see
+// Default kernel (kernel_flag 0): the nonzero-split stream kernel (see
 // csr_stream_kernel); matrices with long runs of empty rows fall back to
-// merge-path.  kernel_flag 2: merge-path.  The (row end, nonzero)
+// merge-path.  kernel_flag 3: the row-block kernel for matrices whose rows
+// are all short (csr_rowblock_kernel; one launch, no fix-up).  kernel_flag 2: merge-path.  The (row end, nonzero)
 // merge sequence is cut into equal tiles of kTile items, so every CTA does the
 // same work whatever the row lengths (power-law rows up to 50k nonzeros and
 // empty rows alike).  A CTA stages its nonzeros' products a_ij * x_j into
@@ -17,8 +18,12 @@
 //
 // kernel_flag 1: vector-per-row kernel, `lanes` threads per row (2..32,
 // chosen from the mean row length, or set by the autotuner).
+#include <type_traits>
+
 #include "common.cuh"
 #include "plan.cuh"
+#include "bulk.cuh"
+#include "primitives.cuh"
 #include "spmv_common.cuh"
 #include "serve.cuh"
 
@@ -367,8 +372,345 @@ sspmv_status launch_vector(const sspmv_csr *A, Plan *p, V alpha, const V *x, int
     }
 }
 
+// ----------------------------------------------------- row-block kernel --
+// kernel_flag 3: short rows, one launch, streamed by the copy engine.
+//
+// The rows are cut into blocks of whole rows: row r opens a block when its
+// first nonzero lies in another window of `window` nonzeros than row r - 1's,
+// or r is a multiple of kRbRows.  A block therefore holds at most kRbRows
+// rows and, with no row longer than kRbMaxRow, at most window + kRbMaxRow - 1
+// nonzeros, and no row crosses two blocks: the CTA that takes a block
+// finishes its rows itself, with no carries and no fix-up launch (a second
+// launch costs about as much as the whole SpMV of an 84 MB matrix).
+//
+// The grid is persistent (every SM full), CTA g taking blocks g, g + G, ...
+// Thread 0 streams each block's row offsets, columns and values into one of
+// kRbStages shared-memory stages with three bulk copies (cp.async.bulk, the
+// copy engine) completed on the stage's mbarrier, kRbStages blocks ahead of
+// the CTA's threads: the matrix moves like a copy, with no per-element load
+// instructions and no load latency on the threads' path.  The threads then
+// gather x for the block's nonzeros (all gathers of a thread in flight
+// together), overwrite each value with its product, and each thread sums its
+// rows' products in row order.  The bulk copies cover the 16-byte aligned
+// interior of each run; the few elements at its ragged ends are read with
+// plain loads.  Deterministic.  Matrices with a row longer than kRbMaxRow use
+// the stream kernel instead, and so do arrays not 16-byte aligned.
+constexpr int kRbRows = 1024;
+constexpr int kRbMaxRow = 64;
+constexpr int kRbDefaultWindow = 1024;
+constexpr int kRbStages = 2;
+
+// Count of bounded waits that gave up (a copy that never completed) in this
+// file's kernels since the library was loaded; read by sspmv_wait_timeouts.
+__device__ unsigned long long g_csr_wait_timeouts = 0;
+
+__global__ void rowblock_flags(int m, int lg_window, const int32_t *__restrict__ rp, int32_t *__restrict__ flag) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= m) return;
+    flag[r] = (r % kRbRows == 0 || (rp[r] >> lg_window) != (rp[r - 1] >> lg_window)) ? 1 : 0;
+}
+
+__global__ void rowblock_starts(int m, int nnz, int lg_window, int nb, const int32_t *__restrict__ rp,
+                                const int32_t *__restrict__ pos, int2 *__restrict__ blocks) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r == 0) blocks[nb] = make_int2(m, nnz);
+    if (r >= m) return;
+    const bool opens = r % kRbRows == 0 || (rp[r] >> lg_window) != (rp[r - 1] >> lg_window);
+    if (opens) blocks[pos[r]] = make_int2((int)r, rp[r]);
+}
+
+// Shared-memory layout of one stage (element capacities; every region starts
+// on a 16-byte boundary).  A block's run [e0, e1) of an array is copied as
+// the 16-byte aligned superset [e0 rounded down, e1 rounded up) -- its
+// neighbours' elements ride along -- and element e sits at index
+// e - (e0 rounded down), so a region holds the longest run plus 2 x 16 bytes.
+template <typename V, int W>
+struct RbStage {
+    static constexpr int kNz = W + kRbMaxRow + 8;        // columns and values
+    static constexpr int kRp = kRbRows + 1 + 7;          // row offsets
+    static constexpr size_t kValBytes = (size_t)kNz * sizeof(V);
+    static constexpr size_t kColBytes = (size_t)kNz * 4;
+    static constexpr size_t kRpBytes = (size_t)kRp * 4;
+    static constexpr size_t kBytes = kValBytes + kColBytes + kRpBytes + 32;  // + header
+};
+
+template <typename V, int W>
+constexpr size_t rowblock_smem() {
+    return kRbStages * RbStage<V, W>::kBytes + kRbStages * sizeof(uint64_t);
+}
+
+// [a, end) = [lo rounded down, hi rounded up) to 16 bytes, cut at the array's
+// last 16-byte boundary (elements beyond it, at most 15 bytes, are read with
+// plain loads: a copy never reads past the array).
+template <int E>
+__device__ __forceinline__ void copy_span(int64_t lo, int64_t hi, int64_t n, int64_t &a, int64_t &end) {
+    constexpr int64_t per = 16 / E;
+    a = lo / per * per;
+    end = min((hi + per - 1) / per * per, n / per * per);
+}
+
+template <typename V, int W, bool PLAIN>
+__global__ void __launch_bounds__(kBlock) csr_rowblock_kernel(int64_t nb, int m, int64_t nnz,
+                                                              const int2 *__restrict__ blocks,
+                                                              const int32_t *__restrict__ rp,
+                                                              const int32_t *__restrict__ col,
+                                                              const V *__restrict__ val, const V *__restrict__ x,
+                                                              int64_t ldx, V alpha, V beta, V *__restrict__ y,
+                                                              int64_t ldy) {
+    using St = RbStage<V, W>;
+    constexpr int kPer = (W + kRbMaxRow + kBlock - 1) / kBlock;
+    extern __shared__ __align__(16) unsigned char rb_smem[];
+    uint64_t *bars = reinterpret_cast<uint64_t *>(rb_smem + kRbStages * St::kBytes);
+    auto sval = [&](int s) { return reinterpret_cast<V *>(rb_smem + s * St::kBytes); };
+    auto scol = [&](int s) { return reinterpret_cast<int32_t *>(rb_smem + s * St::kBytes + St::kValBytes); };
+    auto srp = [&](int s) {
+        return reinterpret_cast<int32_t *>(rb_smem + s * St::kBytes + St::kValBytes + St::kColBytes);
+    };
+    auto shdr = [&](int s) {
+        return reinterpret_cast<int32_t *>(rb_smem + s * St::kBytes + St::kValBytes + St::kColBytes + St::kRpBytes);
+    };
+    const int t = threadIdx.x;
+    const int64_t G = gridDim.x;
+    const int64_t g = blockIdx.x;
+
+    // Thread 0: start the copies of the CTA's k-th block (bounds lo, hi) into
+    // stage k % kRbStages.
+    auto issue = [&](int64_t k, int2 lo, int2 hi) {
+        const int64_t b = g + k * G;
+        if (b >= nb) return;
+        const int s = (int)(k % kRbStages);
+        int64_t av, ve, ac, ce, ap, pe;
+        copy_span<sizeof(V)>(lo.y, hi.y, nnz, av, ve);
+        copy_span<4>(lo.y, hi.y, nnz, ac, ce);
+        copy_span<4>(lo.x, (int64_t)hi.x + 1, (int64_t)m + 1, ap, pe);
+        int32_t *h = shdr(s);
+        h[0] = lo.x;
+        h[1] = hi.x - lo.x;
+        h[2] = lo.y;
+        h[3] = hi.y - lo.y;
+        h[4] = (hi.y > ve || hi.y > ce || (int64_t)hi.x + 1 > pe) ? 1 : 0;  // part of a run past the copies
+        uint32_t tx = 0;
+        tx += ve > av ? (uint32_t)((ve - av) * sizeof(V)) : 0u;
+        tx += ce > ac ? (uint32_t)((ce - ac) * 4) : 0u;
+        tx += pe > ap ? (uint32_t)((pe - ap) * 4) : 0u;
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&bars[s], tx);
+        if (ve > av) bulk_g2s(sval(s), val + av, (uint32_t)((ve - av) * sizeof(V)), &bars[s]);
+        if (ce > ac) bulk_g2s(scol(s), col + ac, (uint32_t)((ce - ac) * 4), &bars[s]);
+        if (pe > ap) bulk_g2s(srp(s), rp + ap, (uint32_t)((pe - ap) * 4), &bars[s]);
+    };
+
+    if (t == 0) {
+        for (int s = 0; s < kRbStages; s++) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (t == 0)
+        for (int k = 0; k < kRbStages; k++)
+            if (g + k * G < nb) issue(k, blocks[g + k * G], blocks[g + k * G + 1]);
+
+    for (int64_t k = 0;; k++) {
+        const int64_t b = g + k * G;
+        if (b >= nb) break;
+        const int s = (int)(k % kRbStages);
+        const uint32_t parity = (uint32_t)((k / kRbStages) & 1);
+        // bounds of the block this iteration's stage takes next, loaded now so
+        // their latency is spent under this block's work
+        const int64_t bn = b + kRbStages * G;
+        int2 nlo = make_int2(0, 0), nhi = make_int2(0, 0);
+        if (t == 0 && bn < nb) {
+            nlo = blocks[bn];
+            nhi = blocks[bn + 1];
+        }
+        // One thread polls; the others sleep at the barrier, then take the
+        // completed phase themselves (one poll, for its acquire).
+        const bool ok = __syncthreads_and(t == 0 ? mbar_wait(&bars[s], parity) : true);
+        if (!ok) {
+            // A copy did not complete: record it, wait (bounded) for the
+            // CTA's other copies in flight, and leave.
+            if (t == 0) {
+                atomicAdd(&g_csr_wait_timeouts, 1ull);
+                for (int64_t k2 = k + 1; k2 < k + kRbStages && g + k2 * G < nb; k2++)
+                    mbar_wait(&bars[k2 % kRbStages], (uint32_t)((k2 / kRbStages) & 1));
+            }
+            return;
+        }
+        if (t != 0) mbar_try_wait(&bars[s], parity);
+        const int32_t *h = shdr(s);
+        const int r0 = h[0], nr = h[1], e0 = h[2], ne = h[3];
+        const bool ragged = h[4] != 0;  // the array's last block: read its tail from global memory
+        constexpr int kPerV = 16 / (int)sizeof(V);
+        const int av = e0 / kPerV * kPerV, ac = e0 / 4 * 4, ap = r0 / 4 * 4;
+        V *vs = sval(s);
+        const int32_t *cs = scol(s), *ps = srp(s);
+        const int64_t vend = nnz / kPerV * kPerV, cend = nnz / 4 * 4, pend = ((int64_t)m + 1) / 4 * 4;
+        if (ne > 0) {
+            const int last = ne - 1;
+            int c[kPer];
+            V a[kPer];
+#pragma unroll
+            for (int j = 0; j < kPer; j++) {
+                // past the block's end: the last column again (a valid gather
+                // kept in flight with the others) and a zero value; each
+                // thread reads only values it overwrites itself
+                const int i = t + j * kBlock;
+                const int e = e0 + min(i, last);
+                if (!ragged) {
+                    c[j] = cs[e - ac];
+                    a[j] = i > last ? V(0) : vs[e - av];
+                } else {
+                    c[j] = e < cend ? cs[e - ac] : ld_stream(col + e);
+                    a[j] = i > last ? V(0) : e < vend ? vs[e - av] : ld_stream(val + e);
+                }
+            }
+            V xv[kPer];
+#pragma unroll
+            for (int j = 0; j < kPer; j++) xv[j] = ld_x(x + (int64_t)c[j] * ldx);
+#pragma unroll
+            for (int j = 0; j < kPer; j++) {
+                const int i = t + j * kBlock;
+                if (i < ne) vs[e0 + i - av] = a[j] * xv[j];
+            }
+        }
+        __syncthreads();
+        // Row sums: L lanes per row, L from the block's mean row length, so
+        // that a warp's lanes read neighbouring products (one lane per row of
+        // 32 nonzeros would put all 32 lanes of a warp on one bank).
+        auto rows = [&](auto lanes) {
+            constexpr int L = decltype(lanes)::value;
+            const int lane = t & 31, sub = lane % L;
+            for (int base = (t >> 5) * (32 / L); base < nr; base += kBlock / L) {
+                const int i = base + lane / L;
+                V sum = V(0);
+                int r = r0 + i;
+                if (i < nr) {
+                    int rs, re;
+                    if (!ragged) {
+                        rs = ps[r - ap];
+                        re = ps[r + 1 - ap];
+                    } else {
+                        rs = r < pend ? ps[r - ap] : ld_stream(rp + r);
+                        re = r + 1 < pend ? ps[r + 1 - ap] : ld_stream(rp + r + 1);
+                    }
+                    for (int e = rs + sub; e < re; e += L) sum += vs[e - av];
+                }
+                if constexpr (L > 1) sum = warp_sum(sum, L);
+                if (i < nr && sub == 0) {
+                    V *yp = y + (int64_t)r * ldy;
+                    *yp = row_out(PLAIN, alpha, sum, beta, yp);
+                }
+            }
+        };
+        const int mean = nr > 0 ? ne / nr : 0;
+        if (mean < 6) rows(std::integral_constant<int, 1>());
+        else if (mean < 12) rows(std::integral_constant<int, 2>());
+        else if (mean < 24) rows(std::integral_constant<int, 4>());
+        else rows(std::integral_constant<int, 8>());
+        __syncthreads();  // stage s free
+        if (t == 0) issue(k + kRbStages, nlo, nhi);
+    }
+}
+
+// Plan slots of the row-block kernel: extra[4] blocks (int2, nb + 1),
+// extra_i[4] = nb (-1: a row longer than kRbMaxRow, kernel not usable),
+// extra_i[5] = longest row, extra_i[6] = window of the blocks built.
+sspmv_status ensure_rowblock_plan(const sspmv_csr *A, Plan *p, int window, sspmv_stream_t s) {
+    if (p->extra_i[4] != 0 && (p->extra_i[4] < 0 || p->extra_i[6] == window)) return SSPMV_OK;
+    std::lock_guard<PlanMutex> g(plan_mutex());
+    if (p->extra_i[4] != 0 && (p->extra_i[4] < 0 || p->extra_i[6] == window)) return SSPMV_OK;
+    const int64_t m = A->f.num_rows, nnz = A->f.num_nnzs;
+    int32_t longest = 0;
+    SSPMV_TRY(max_row_length(A->row_offset, m, &longest, s));
+    p->extra_i[5] = longest;
+    if (longest > kRbMaxRow) {
+        p->extra_i[4] = -1;
+        return SSPMV_OK;
+    }
+    int lg = 0;
+    while ((1 << lg) < window) lg++;
+    int32_t *pos = nullptr;
+    SSPMV_TRY(dalloc(&pos, (size_t)m, s));
+    rowblock_flags<<<grid_for(m, 256), 256, 0, cu(s)>>>((int)m, lg, A->row_offset, pos);
+    SSPMV_LAUNCH_CHECK();
+    int32_t nb = 0;
+    sspmv_status st = exclusive_scan_i32(pos, pos, m, &nb, s);
+    if (st != SSPMV_OK) {
+        dfree(pos, s);
+        return st;
+    }
+    int2 *blocks = nullptr;
+    st = dalloc(&blocks, (size_t)nb + 1, s);
+    if (st != SSPMV_OK) {
+        dfree(pos, s);
+        return st;
+    }
+    rowblock_starts<<<grid_for(m, 256), 256, 0, cu(s)>>>((int)m, (int)nnz, lg, nb, A->row_offset, pos, blocks);
+    SSPMV_LAUNCH_CHECK();
+    dfree(pos, s);
+    if (p->extra[4]) dfree(p->extra[4], s);
+    p->extra[4] = blocks;
+    p->extra_i[6] = window;
+    p->extra_i[4] = nb;
+    return SSPMV_OK;
+}
+
+template <typename V, int W, bool PLAIN>
+sspmv_status go_rowblock_k(const sspmv_csr *A, const int2 *blocks, int64_t nb, V alpha, const V *x, int64_t ldx,
+                           V beta, V *y, int64_t ldy, sspmv_stream_t s) {
+    constexpr size_t smem = rowblock_smem<V, W>();
+    static int per_sm = 0;  // resident CTAs per SM (set once per instantiation)
+    if (per_sm == 0) {
+        SSPMV_CUDA_TRY(cudaFuncSetAttribute(csr_rowblock_kernel<V, W, PLAIN>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int n = 0;
+        SSPMV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, csr_rowblock_kernel<V, W, PLAIN>, kBlock,
+                                                                     smem));
+        per_sm = n > 0 ? n : 1;
+    }
+    const int64_t grid = std::min<int64_t>(nb, (int64_t)num_sms() * per_sm);
+    csr_rowblock_kernel<V, W, PLAIN><<<(unsigned)grid, kBlock, smem, cu(s)>>>(
+        nb, (int)A->f.num_rows, A->f.num_nnzs, blocks, A->row_offset, A->col_index, (const V *)A->values, x, ldx,
+        alpha, beta, y, ldy);
+    SSPMV_LAUNCH_CHECK();
+    return SSPMV_OK;
+}
+
+template <typename V, int W>
+sspmv_status go_rowblock(const sspmv_csr *A, const int2 *blocks, int64_t nb, V alpha, const V *x, int64_t ldx,
+                         V beta, V *y, int64_t ldy, sspmv_stream_t s) {
+    if (alpha == V(1) && beta == V(0))
+        return go_rowblock_k<V, W, true>(A, blocks, nb, alpha, x, ldx, beta, y, ldy, s);
+    return go_rowblock_k<V, W, false>(A, blocks, nb, alpha, x, ldx, beta, y, ldy, s);
+}
+
+// Sets *launched = false (nothing launched) when the matrix has a row longer
+// than kRbMaxRow or arrays that are not 16-byte aligned; the caller then runs
+// another kernel.
+template <typename V>
+sspmv_status launch_rowblock(const sspmv_csr *A, Plan *p, V alpha, const V *x, int64_t ldx, V beta, V *y,
+                             int64_t ldy, sspmv_stream_t s, bool *launched) {
+    *launched = false;
+    const uintptr_t bases = reinterpret_cast<uintptr_t>(A->row_offset) | reinterpret_cast<uintptr_t>(A->col_index) |
+                            reinterpret_cast<uintptr_t>(A->values);
+    if ((bases & 15) != 0) return SSPMV_OK;
+    int window = p->param > 0 ? p->param : kRbDefaultWindow;
+    if (window != 512 && window != 1024 && window != 2048 && window != 4096) window = kRbDefaultWindow;
+    SSPMV_TRY(ensure_rowblock_plan(A, p, window, s));
+    if (p->extra_i[4] < 0) return SSPMV_OK;
+    const int2 *blocks = (const int2 *)p->extra[4];
+    const int64_t nb = p->extra_i[4];
+    switch (window) {
+    case 512: SSPMV_TRY((go_rowblock<V, 512>(A, blocks, nb, alpha, x, ldx, beta, y, ldy, s))); break;
+    case 2048: SSPMV_TRY((go_rowblock<V, 2048>(A, blocks, nb, alpha, x, ldx, beta, y, ldy, s))); break;
+    case 4096: SSPMV_TRY((go_rowblock<V, 4096>(A, blocks, nb, alpha, x, ldx, beta, y, ldy, s))); break;
+    default: SSPMV_TRY((go_rowblock<V, 1024>(A, blocks, nb, alpha, x, ldx, beta, y, ldy, s))); break;
+    }
+    *launched = true;
+    return SSPMV_OK;
+}
+
 // ------------------------------------------------------- stream kernel --
-// kernel_flag 3: nonzero-split "stream" kernel.  A warp takes 256 consecutive
+// kernel_flag 0: nonzero-split "stream" kernel.  A warp takes 256 consecutive
 // nonzeros, lane l the 8 at 8l (vector loads of columns and values, all 8
 // gathers issued before use for k <= 2).  A lane finds the row of its first
 // nonzero by binary search inside the warp's row range (row_start of the
@@ -1142,6 +1484,13 @@ sspmv_status csr_pass(const sspmv_csr *A, Plan *p, V alpha, const V *x, int64_t 
                       int64_t ldy, sspmv_stream_t s) {
     if (A->f.kernel_flag == 1) return launch_vector<V, K>(A, p, alpha, x, ldx, beta, y, ldy, s);
     if (A->f.kernel_flag == 2) return launch_merge<V, K>(A, p, alpha, x, ldx, beta, y, ldy, s);
+    if constexpr (K == 1) {
+        if (A->f.kernel_flag == 3) {
+            bool launched = false;
+            SSPMV_TRY(launch_rowblock<V>(A, p, alpha, x, ldx, beta, y, ldy, s, &launched));
+            if (launched) return SSPMV_OK;
+        }
+    }
     return launch_stream<V, K>(A, p, alpha, x, ldx, beta, y, ldy, s);
 }
 
@@ -1371,4 +1720,12 @@ extern "C" sspmv_status sspmv_LeSpMV_csr_noalloc(double alpha, const sspmv_csr *
         }
         return SSPMV_OK;
     });
+}
+
+extern "C" sspmv_status sspmv_wait_timeouts(int64_t *count) {
+    if (!count) return fail(SSPMV_INVALID_ARG, "null output");
+    unsigned long long v = 0;
+    SSPMV_CUDA_TRY(cudaMemcpyFromSymbol(&v, g_csr_wait_timeouts, sizeof(v)));
+    *count = (int64_t)v;
+    return SSPMV_OK;
 }

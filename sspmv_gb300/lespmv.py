@@ -18,6 +18,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import Csr, F32, F64, SSPMVError, call, lib
+from .formats import FORMATS, bsr_block_for, feasible_host  # noqa: F401  (re-exported)
 from .synth import HostCSR
 
 RowMajor, ColMajor = _lib.ROW_MAJOR, _lib.COL_MAJOR
@@ -365,6 +366,14 @@ def fp64_ceiling(stream=None) -> float:
     return rate.value
 
 
+def wait_timeouts() -> int:
+    """Bounded device waits that gave up since the library was loaded (0 in
+    every correct run)."""
+    n = C.c_int64()
+    call("sspmv_wait_timeouts", C.byref(n))
+    return int(n.value)
+
+
 def sum_csr_duplicates(A: HostCSR) -> HostCSR:
     """sum_csr_duplicates (include/sparse_operation.h:22-73) on a copy of A:
     equal columns of a row summed, columns in reverse order of first
@@ -494,38 +503,8 @@ def LeSpMV_csr(alpha, A: CSR_Matrix, x, beta, y, stream=None) -> None:
     LeSpMV(alpha, A, x, beta, y, stream)
 
 
-# Formats the library builds, in benchmark order.
-FORMATS = ["csr", "coo", "ell", "sell", "sell_c_sigma", "sell_c_R", "dia", "bsr", "csr5"]
-# Formats the smoke check converts from CSR (besides CSR itself).
+# Smoke-check formats converted from CSR (besides CSR itself).
 SMOKE_FORMATS: list[str] = ["coo", "ell", "sell", "sell_c_sigma", "sell_c_R", "bsr", "csr5"]
-
-
-def bsr_block_for(A: HostCSR) -> tuple[int, int]:
-    """Block shape used for a host matrix when none is given: 4x4."""
-    return 4, 4
-
-
-def feasible_host(fmt: str, A: HostCSR) -> tuple[bool, str]:
-    """Whether `fmt` is worth building for A (padding within 4x the CSR size,
-    DIA within the reference's 10240-diagonal limit)."""
-    if fmt in ("csr", "coo", "csr5", "sell", "sell_c_sigma", "sell_c_R"):
-        return True, ""
-    m, nnz = A.num_rows, max(A.nnz, 1)
-    lens = np.diff(A.row_offset)
-    if fmt == "ell":
-        w = int(lens.max()) if m else 0
-        return (m * w <= 4 * nnz, f"ELL width {w} pads {m * w / nnz:.1f}x")
-    if fmt == "dia":
-        rows = np.repeat(np.arange(m, dtype=np.int64), lens)
-        nd = int(np.count_nonzero(np.bincount(A.col_index.astype(np.int64) - rows + m, minlength=1)))
-        return (nd <= 10240, f"{nd} diagonals > 10240")
-    if fmt == "bsr":
-        r, c = bsr_block_for(A)
-        rows = np.repeat(np.arange(m, dtype=np.int64), lens) // r
-        keys = rows * ((A.num_cols + c - 1) // c) + A.col_index // c
-        nnzb = len(np.unique(keys))
-        return (nnzb * r * c <= 4 * nnz, f"BSR {r}x{c} fill {nnzb * r * c / nnz:.1f}x")
-    return False, "unknown format"
 
 
 def count_blocks(csr: CSR_Matrix, r: int, c: int, stream=None) -> int:

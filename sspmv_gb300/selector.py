@@ -134,13 +134,14 @@ def _time_ms(M, x, y, flush, reps=3):
 def label_matrix(A: HostCSR, flush=None) -> dict:
     """Measured best time (ms) and parameters of every format on A (None when
     the format is infeasible), and the raw features."""
+    from .autotune import L2Flush
     import torch
     from . import lespmv as L
     csr = L.csr_from_host(A)
     x = torch.from_numpy(synth.vector(A.num_cols, 0, A.values.dtype)).cuda()
     y = torch.zeros(A.num_rows, dtype=x.dtype, device="cuda")
     if flush is None:
-        flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+        flush = L2Flush("cuda")
     out = {"times": {}, "params": {}}
     t0 = time.perf_counter()
     out["raw"] = raw_features(csr).tolist()
@@ -189,6 +190,7 @@ def label_matrix(A: HostCSR, flush=None) -> dict:
 def build_dataset(path: str | Path, count: int, start: int = 0, seed: int = 0, log=None) -> None:
     """Appends label records of matrices start .. start+count-1 to a JSONL
     file (matrices already present are skipped, so runs can be resumed)."""
+    from .autotune import L2Flush
     import torch
     log = log or (lambda *a: None)
     path = Path(path)
@@ -197,7 +199,7 @@ def build_dataset(path: str | Path, count: int, start: int = 0, seed: int = 0, l
         for ln in path.read_text().splitlines():
             if ln.strip():
                 done.add(json.loads(ln)["i"])
-    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+    flush = L2Flush("cuda")
     with open(path, "a") as f:
         for i in range(start, start + count):
             if i in done:

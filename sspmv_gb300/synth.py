@@ -1,4 +1,9 @@
-"""Seeded synthetic matrices (host side, native generator in libsspmv.so).
+"""Seeded synthetic matrices (host side).
+
+The generator is sspmv_gb300/csrc/synth.cpp.  It is exported by libsspmv.so
+(the C ABI's sspmv_synth_*) and also built on its own, host-only, as
+lib/libsspmv_synth.so, which is what this module loads: the CPU legs of the
+benchmark generate their inputs without loading the GPU library.
 
 The suite's workloads, by name and size:
   laplacian_1024   2-D 5-point Laplacian on a 1024 x 1024 grid (N=1,048,576)
@@ -16,10 +21,39 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from . import _lib
-from ._lib import SynthParams, lib
+from pathlib import Path
+
+_LIB_PATH = Path(__file__).resolve().parent / "lib" / "libsspmv_synth.so"
 
 LAPLACIAN2D, BANDED, POWERLAW, BLOCK, UNIFORM = range(5)
+
+
+class SynthParams(C.Structure):
+    """sspmv_synth_params (include/sspmv.h)."""
+    _fields_ = [("family", C.c_int32), ("num_offsets", C.c_int32), ("num_rows", C.c_int64),
+                ("num_cols", C.c_int64), ("grid", C.c_int64), ("offsets", C.c_int64 * 32),
+                ("alpha", C.c_double), ("mean", C.c_double), ("cap", C.c_int64),
+                ("block_dim", C.c_int64), ("num_blocks", C.c_int64), ("per_row", C.c_int64),
+                ("empty_row_frac", C.c_double)]
+
+
+def _load():
+    if not _LIB_PATH.exists():
+        raise ImportError(f"libsspmv_synth.so is not built ({_LIB_PATH}); run __graft_entry__.build() "
+                          "or python -m sspmv_gb300.build")
+    h = C.CDLL(str(_LIB_PATH))
+    vp = C.c_void_p
+    for name, res, args in (("sspmv_synth_row_offsets", C.c_int64, [C.POINTER(SynthParams), C.c_uint64, vp]),
+                            ("sspmv_synth_fill_f64", C.c_int, [C.POINTER(SynthParams), C.c_uint64, vp, vp, vp]),
+                            ("sspmv_synth_fill_f32", C.c_int, [C.POINTER(SynthParams), C.c_uint64, vp, vp, vp]),
+                            ("sspmv_synth_vector_f64", None, [C.c_int64, C.c_uint64, vp]),
+                            ("sspmv_synth_vector_f32", None, [C.c_int64, C.c_uint64, vp])):
+        f = getattr(h, name)
+        f.restype, f.argtypes = res, args
+    return h
+
+
+lib = _load()
 
 
 def laplacian2d(grid: int) -> SynthParams:
@@ -121,4 +155,4 @@ def load(name: str, seed: int = 1, dtype=np.float64) -> HostCSR:
 
 
 __all__ = ["laplacian2d", "banded", "powerlaw", "block", "uniform", "generate", "vector", "load",
-           "WORKLOADS", "HostCSR", "_lib"]
+           "WORKLOADS", "HostCSR", "SynthParams"]

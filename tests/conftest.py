@@ -15,6 +15,8 @@ def pytest_configure(config):
     from sspmv_gb300 import build as _b
     if not _b.LIB.exists():
         _b.build_library()
+    if not _b.SYNTH_LIB.exists():
+        _b.build_synth()
     if not (ROOT / "oracle" / "liboracle.so").exists():
         _b.build_oracle(with_reference=False)
 

@@ -68,6 +68,78 @@ def test_csr_spmm_families(fam, k, dt, oracle_lib):
         assert ok, f"{fam} k={k} flag={flag}: max normalised error {mx}"
 
 
+def _short_rows(s, case):
+    """Matrices for the row-block kernel: rows of at most 64 nonzeros, runs
+    of empty rows (more than one 1024-row block of them), rows of exactly 64,
+    blocks that end on a window boundary."""
+    if case == "uniform64_empty":
+        return s.uniform(30000, 64, 0.3)
+    if case == "uniform1":
+        return s.uniform(70000, 1)
+    if case == "lap":
+        return s.laplacian2d(257)
+    if case == "banded":
+        return s.banded(50000)
+    if case == "block":
+        return s.block(50000, 4, 12000)
+    return s.powerlaw(40000, 1.8, 8.0, 64, 0.05)
+
+
+def _empty_runs(dt):
+    """Runs of 2500 and 3000 empty rows between rows of 1..64 nonzeros, and
+    empty last rows."""
+    rng = np.random.default_rng(11)
+    lens = np.concatenate([np.zeros(2500, np.int64), rng.integers(1, 65, 4000), np.zeros(3000, np.int64),
+                           rng.integers(0, 4, 5000), np.zeros(700, np.int64)])
+    m = n = len(lens)
+    rp = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    col = np.concatenate([np.sort(rng.choice(n, int(k), replace=False)) for k in lens if k] or
+                         [np.zeros(0, np.int64)]).astype(np.int32)
+    from sspmv_gb300.synth import HostCSR
+    return HostCSR(m, n, rp, col, rng.uniform(-1, 1, int(rp[-1])).astype(dt))
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
+@pytest.mark.parametrize("window", [0, 512, 1024, 2048, 4096])
+@pytest.mark.parametrize("case", ["uniform64_empty", "uniform1", "lap", "banded", "block", "powerlaw_cap64",
+                                  "empty_runs"])
+def test_csr_rowblock(case, window, dt, oracle_lib):
+    """kernel_flag 3 (row-block kernel) on every window, with alpha/beta and
+    with alpha = 1, beta = 0 (the y = sum instantiation, y filled with NaN)."""
+    from sspmv_gb300 import synth
+    from sspmv_gb300.lespmv import LeSpMV_csr
+    A = _empty_runs(dt) if case == "empty_runs" else synth.generate(_short_rows(synth, case), 3, dt)
+    assert np.diff(A.row_offset).max() <= 64
+    x = synth.vector(A.num_cols, 0, dt)
+    y0 = synth.vector(A.num_rows, 5, dt)
+    M = _csr(A)
+    M.set_kernel(3, window)
+    for alpha, beta, init in ((ALPHA, BETA, y0), (1.0, 0.0, np.full(A.num_rows, np.nan, dt))):
+        y = to_dev(init)
+        LeSpMV_csr(alpha, M, to_dev(x), beta, y)
+        yg = to_host(y)
+        y64, absum = oracle_lib.spmm_ref(A, x, alpha, beta, y0 if beta else None)
+        ok, mx, _ = tolerance_ok(yg, y64, absum, np.diff(A.row_offset), dt, alpha, beta, y0 if beta else None)
+        assert ok, f"{case} window {window} alpha {alpha}: max normalised error {mx}"
+    from sspmv_gb300.lespmv import wait_timeouts
+    assert wait_timeouts() == 0
+
+
+def test_csr_rowblock_falls_back_on_long_rows(oracle_lib):
+    """A row longer than 64 nonzeros: kernel_flag 3 runs the default kernel."""
+    from sspmv_gb300 import synth
+    from sspmv_gb300.lespmv import LeSpMV_csr
+    A = synth.generate(synth.powerlaw(20000, 1.8, 16, 5000), 4)
+    x = synth.vector(A.num_cols, 0)
+    M = _csr(A)
+    M.set_kernel(3, 0)
+    y = to_dev(np.zeros(A.num_rows))
+    LeSpMV_csr(1.0, M, to_dev(x), 0.0, y)
+    y64, absum = oracle_lib.spmm_ref(A, x, 1.0, 0.0)
+    ok, mx, _ = tolerance_ok(to_host(y), y64, absum, np.diff(A.row_offset), np.float64)
+    assert ok, mx
+
+
 def test_csr_beta_zero_ignores_nan_y(oracle_lib):
     from sspmv_gb300 import synth
     from sspmv_gb300.lespmv import LeSpMV_csr
