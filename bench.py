@@ -64,11 +64,24 @@ def parse_args(argv=None):
     ap.add_argument("--kernel", action="append", default=[],
                     help="pin a format's kernel as FMT:FLAG:PARAM (repeatable; that format is not tuned)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
-    ap.add_argument("--no-large", action="store_true", help="skip the power-law 16M SELL-c-sigma vs CSR section")
+    ap.add_argument("--no-large", action="store_true", help="skip the Laplacian and the power-law 16M SELL-c-sigma vs CSR sections")
     ap.add_argument("--no-serving", action="store_true", help="skip the request-server section")
+    ap.add_argument("--sections", default="suite,laplacian,large,serving",
+                    help="sections to run: suite (the timed line), laplacian (1024^2 from .mtx), large "
+                         "(power-law 16M), serving; e.g. --sections laplacian for a profiling run")
     ap.add_argument("--detail", default=str(ROOT / "gpurun_out" / "bench_detail.json"),
                     help="file for the full result (per-format table, sweeps); '' to skip")
     return ap.parse_args(argv)
+
+
+def sections(args) -> set[str]:
+    """The sections a run includes (--sections, less the --no-* ones)."""
+    out = {x for x in args.sections.split(",") if x}
+    if args.no_large:
+        out -= {"laplacian", "large"}
+    if args.no_serving:
+        out.discard("serving")
+    return out
 
 
 _T0 = time.perf_counter()
@@ -150,6 +163,51 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+# ------------------------------------------------------------ probes ------
+class Probes:
+    """The benchmark's measurement probes (sspmv_gb300/csrc/probe/calibrate.cu,
+    lib/libsspmv_probe.so): the random-gather rate and the FP64 FMA rate of
+    the device, the ceilings that bound SpMV on random-column matrices and
+    FP64 SpMV where HBM bytes do not."""
+
+    def __init__(self):
+        import ctypes as C
+        from sspmv_gb300 import _lib  # loads libsspmv.so, which the probe library links
+        self.C = C
+        self.call = _lib.call
+        path = ROOT / "sspmv_gb300" / "lib" / "libsspmv_probe.so"
+        if not path.exists():
+            raise ImportError(f"{path} is not built; run __graft_entry__.build()")
+        h = C.CDLL(str(path))
+        h.sspmv_gather_ceiling.restype = C.c_int
+        h.sspmv_gather_ceiling.argtypes = [C.c_int32, C.c_int64, C.c_int64, C.POINTER(C.c_double),
+                                           C.POINTER(C.c_double), C.c_void_p]
+        h.sspmv_fp64_ceiling.restype = C.c_int
+        h.sspmv_fp64_ceiling.argtypes = [C.POINTER(C.c_double), C.c_void_p]
+        self.h = h
+
+    def _check(self, st, what):
+        from sspmv_gb300 import _lib
+        _lib.check(st, what)
+
+    def gather_ceiling(self, dtype, num_cols, num_gathers):
+        """(gathers per second, checksum) of random gathers from a vector of
+        num_cols values, num_gathers indices streamed once."""
+        C = self.C
+        rate, chk = C.c_double(0.0), C.c_double(0.0)
+        vt = 1 if np.dtype(dtype) == np.float64 else 0
+        self._check(self.h.sspmv_gather_ceiling(vt, int(num_cols), int(num_gathers), C.byref(rate), C.byref(chk),
+                                                None), "sspmv_gather_ceiling")
+        return rate.value, chk.value
+
+    def fp64_ceiling(self):
+        """FP64 FMAs per second (independent chains)."""
+        C = self.C
+        rate = C.c_double(0.0)
+        self._check(self.h.sspmv_fp64_ceiling(C.byref(rate), None), "sspmv_fp64_ceiling")
+        return rate.value
+
+
 def measured_peak():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -166,12 +224,48 @@ def traffic_table():
 
 # ---------------------------------------------------------------- GPU arm --
 def run_gpu(args, rank, world):
+    """The GPU arm: the timed suite (the result line's value), then the
+    Laplacian, large power-law and serving sections (rank 0)."""
+    import torch
+    secs = sections(args)
+    dev = torch.device("cuda", rank % max(1, torch.cuda.device_count()))
+    torch.cuda.set_device(dev)
+    peak, _ = measured_peak()
+    families = [f for f in args.families.split(",") if f]
+    dtypes = [d for d in args.dtypes.split(",") if d]
+    if "suite" in secs:
+        out = run_suite(args, dev, rank, world)
+    else:
+        out = {"metric": SUITE_METRIC, "value": None, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic", "config": {"sections": sorted(secs)}}
+    lap = large = serving = None
+    full = args.scale == 1.0
+    if rank == 0 and "laplacian" in secs and full:
+        lap = run_laplacian(dev, peak)
+        log("laplacian done")
+    if rank == 0 and "large" in secs and full:
+        large = run_large(dev, peak)
+        log("large done")
+    if rank == 0 and "serving" in secs and full:
+        serving = run_serving()
+        log("serving done")
+    out.update({"laplacian_1024": lap, "large_powerlaw_16M": large, "serving": serving})
+    del families, dtypes
+    return out
+
+
+SUITE_METRIC = "SpMV GB/s (algorithmic bytes / kernel time), all formats x 4 families x {f64,f32}"
+
+
+def run_suite(args, dev, rank, world):
+    """Every feasible (family, format, precision) of the suite, autotuned,
+    one SpMV each per step, timed with CUDA events; parity, e2e, roofline,
+    CPU baseline."""
     import torch
     from sspmv_gb300 import _lib
     from sspmv_gb300 import lespmv as L
 
-    dev = torch.device("cuda", rank % max(1, torch.cuda.device_count()))
-    torch.cuda.set_device(dev)
     families = [f for f in args.families.split(",") if f]
     dtypes = [d for d in args.dtypes.split(",") if d]
     fmts = L.FORMATS if args.formats == "all" else args.formats.split(",")
@@ -313,33 +407,33 @@ def run_gpu(args, rank, world):
         # random column indices: the x gathers, not HBM, bound the kernels; the
         # gather ceiling is measured live for each such matrix's x size and
         # gather count (one gather per nonzero)
-        from sspmv_gb300 import lespmv as L
+        probes = Probes()
         ceiling = {}
         for c, pc in zip(cases, per_case):
             if c["fam"] not in RANDOM_COLUMN_FAMILIES:
                 continue
             key = (c["fam"], c["dt"])
             if key not in ceiling:
-                ceiling[key] = L.gather_ceiling(np_dtype(c["dt"]), c["cols"], min(c["nnz"], 1 << 28))[0]
+                ceiling[key] = probes.gather_ceiling(np_dtype(c["dt"]), c["cols"], min(c["nnz"], 1 << 28))[0]
             pc["gather_frac"] = round(c["nnz"] / (pc["ms"] * 1e-3) / ceiling[key], 4)
         # FP64: one FMA per nonzero against the device's measured FP64 FMA rate
-        fma_rate = L.fp64_ceiling()
+        fma_rate = probes.fp64_ceiling()
         for c, pc in zip(cases, per_case):
             if c["dt"] == "f64":
                 pc["fp64_frac"] = round(c["nnz"] / (pc["ms"] * 1e-3) / fma_rate, 4)
         key = (dc["fam"], dc["dt"])
-        rate = ceiling.get(key) or L.gather_ceiling(np_dtype(dc["dt"]), dc["cols"], min(dc["nnz"], 1 << 28))[0]
+        rate = ceiling.get(key) or probes.gather_ceiling(np_dtype(dc["dt"]), dc["cols"], min(dc["nnz"], 1 << 28))[0]
         kernel_rate = dc["nnz"] / (per_case[dom]["ms"] * 1e-3)
         roofline["gather_ceiling"] = {
             "ceiling_gathers_per_s": round(rate, 1), "achieved_gathers_per_s": round(kernel_rate, 1),
             "frac": round(kernel_rate / rate, 4),
             "what": "one x gather per nonzero; ceiling = random gathers from a vector of the same size, "
-                    "indices streamed (sspmv_gather_ceiling)"}
+                    "indices streamed (benchmark probe sspmv_gather_ceiling)"}
         if dc["dt"] == "f64":
             roofline["fp64_ceiling"] = {
                 "ceiling_fmas_per_s": round(fma_rate, 1), "achieved_fmas_per_s": round(kernel_rate, 1),
                 "frac": round(kernel_rate / fma_rate, 4),
-                "what": "one FP64 FMA per nonzero; ceiling = independent FMA chains (sspmv_fp64_ceiling)"}
+                "what": "one FP64 FMA per nonzero; ceiling = independent FMA chains (benchmark probe sspmv_fp64_ceiling)"}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(hosts, families, dtypes, fmts, budget_s=15.0)
@@ -350,17 +444,8 @@ def run_gpu(args, rank, world):
     for c in cases:
         c["csr"].delete()
     del cases, hosts
-    large = serving = lap = None
-    if rank == 0 and not args.no_large and args.scale == 1.0:
-        lap = run_laplacian(dev, peak)
-        log("laplacian done")
-        large = run_large(dev, peak)
-        log("large done")
-    if rank == 0 and not args.no_serving and args.scale == 1.0:
-        serving = run_serving()
-        log("serving done")
     return {
-        "metric": "SpMV GB/s (algorithmic bytes / kernel time), all formats x 4 families x {f64,f32}",
+        "metric": SUITE_METRIC,
         "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64+f32", "data": "synthetic (seeded generator, families of the SpMV suite)",
@@ -370,8 +455,7 @@ def run_gpu(args, rank, world):
                    "skipped": skipped, "scale": args.scale},
         "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches),
         "parity": parity,
-        "wall_s": round(wall, 3), "per_format": per_case, "laplacian_1024": lap, "large_powerlaw_16M": large,
-        "serving": serving,
+        "wall_s": round(wall, 3), "per_format": per_case,
     }
 
 

@@ -208,20 +208,15 @@ const char *sspmv_last_error(void);
 const char *sspmv_version(void);
 /* Number of kernels this library has launched in the process so far. */
 int64_t sspmv_launch_count(void);
-/* Measured ceiling of random gathers from a vector of num_cols values of
- * value_type: num_gathers (rounded down to a multiple of 256) uniformly
- * spread indices streamed once, 8 read-only gathers in flight per lane, the
- * pattern of SpMV on matrices with random column indices.  Best of 5 timed
- * launches after 3 warm-up ones, in gathers per second; checksum (optional)
- * is the sum of the per-thread sums.  A measurement utility of this library
- * (no reference counterpart); allocates and frees its own buffers. */
-sspmv_status sspmv_gather_ceiling(int32_t value_type, int64_t num_cols, int64_t num_gathers,
-                                  double *gathers_per_second, double *checksum, sspmv_stream_t stream);
-/* Measured FP64 fused multiply-add rate of the device (independent chains,
- * best of 5 launches after 3 warm-up ones), in FMAs per second: the bound of
- * FP64 SpMV (one FMA per nonzero) where neither bytes nor gathers bind.
- * A measurement utility of this library (no reference counterpart). */
-sspmv_status sspmv_fp64_ceiling(double *fmas_per_second, sspmv_stream_t stream);
+/* Frees the plan of a matrix (pass &A->f): the per-matrix schedule and carry
+ * buffers the first SpMV builds, which sspmv_delete_<fmt> otherwise frees.
+ * The frees are ordered on `stream` (work queued there before may still use
+ * the plan) and nothing waits for the device; the next SpMV builds a new
+ * plan.  The kernel choice (kernel_flag and the sspmv_set_kernel parameter)
+ * is kept; a nonzero parameter is kept in a host-side record that
+ * sspmv_delete_<fmt> frees.  For callers that wrap arrays per call (sspmv_csr_wrap) and must not
+ * keep state between calls.  No reference counterpart. */
+sspmv_status sspmv_release_plan(sspmv_features *f, sspmv_stream_t stream);
 /* Selects the SpMV kernel of a matrix (pass &A->f): kernel_flag as in each
  * format's LeSpMV entry, param a kernel parameter (0 lets the library
  * choose): CSR vector kernel: lanes per row 2..32; CSR row-block kernel:
@@ -275,8 +270,9 @@ sspmv_status sspmv_spmm_csr(double alpha, const sspmv_csr *A, int32_t k, const v
  * library keeps until exit; no per-matrix plan is built and nothing is
  * allocated.  Limit: num_rows + num_nnzs <= 238,594,048 (116,501 tiles of
  * 2048 merge items); larger matrices return SSPMV_INVALID_ARG.  The first call
- * on a device looks up the array's address with that device current: make it
- * before any stream capture.  All calls share the array: calls that overlap on
+ * on a device (and the first after a cudaDeviceReset of it) looks up the
+ * array's address with that device current: make it before any stream
+ * capture.  All calls share the array: calls that overlap on
  * the GPU race and must be serialised by the caller.  Nothing in the array
  * needs clearing between calls (each call writes every entry it reads). */
 sspmv_status sspmv_LeSpMV_csr_noalloc(double alpha, const sspmv_csr *A, const void *x, double beta, void *y,

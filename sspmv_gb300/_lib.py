@@ -116,8 +116,6 @@ _SIGS = {
     "sspmv_last_error": (C.c_char_p, []),
     "sspmv_version": (C.c_char_p, []),
     "sspmv_launch_count": (_i64, []),
-    "sspmv_gather_ceiling": (_st, [_i32, _i64, _i64, C.POINTER(_d), C.POINTER(_d), _vp]),
-    "sspmv_fp64_ceiling": (_st, [C.POINTER(_d), _vp]),
     "sspmv_set_kernel": (_st, [C.POINTER(Features), _i32, _i32]),
     "sspmv_csr_create": (_st, [C.POINTER(Csr), _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp]),
     "sspmv_csr_wrap": (_st, [C.POINTER(Csr), _i32, _i64, _i64, _i64, _vp, _vp, _vp]),
@@ -127,6 +125,7 @@ _SIGS = {
     "sspmv_spmm_csr": (_st, [_d, C.POINTER(Csr), _i32, _vp, _i64, _d, _vp, _i64, _vp]),
     "sspmv_LeSpMV_csr_noalloc": (_st, [_d, C.POINTER(Csr), _vp, _d, _vp, _vp]),
     "sspmv_wait_timeouts": (_st, [C.POINTER(_i64)]),
+    "sspmv_release_plan": (_st, [C.POINTER(Features), _vp]),
     "sspmv_algorithmic_bytes_csr": (_d, [C.POINTER(Csr), _i32, _i32]),
     "sspmv_reference_bytes_csr": (_d, [C.POINTER(Csr)]),
     "sspmv_read_mtx": (_st, [C.c_char_p, _i32, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64), _vp, _vp, _vp]),

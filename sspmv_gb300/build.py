@@ -78,6 +78,25 @@ def build_library(verbose: bool = False, extra: list[str] | None = None, jobs: i
 
 
 SYNTH_LIB = LIBDIR / "libsspmv_synth.so"
+PROBE_SRC = CSRC / "probe" / "calibrate.cu"
+PROBE_LIB = LIBDIR / "libsspmv_probe.so"
+
+
+def build_probe() -> Path:
+    """lib/libsspmv_probe.so: the benchmark's measurement probes (random
+    gather rate, FP64 FMA rate), linked against libsspmv.so; not part of the
+    library's C ABI."""
+    obj = BUILD / "calibrate.cu.o"
+    newest = max([PROBE_SRC.stat().st_mtime] + [h.stat().st_mtime for h in _headers()])
+    if not PROBE_LIB.exists() or PROBE_LIB.stat().st_mtime < max(newest, LIB.stat().st_mtime):
+        BUILD.mkdir(exist_ok=True)
+        _compile(PROBE_SRC, [])
+        cmd = [NVCC, *ARCH, "-shared", "-o", str(PROBE_LIB), str(obj), f"-L{LIBDIR}", "-lsspmv",
+               "-Xlinker", "-rpath=$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"probe link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return PROBE_LIB
 
 
 def build_synth() -> Path:
@@ -122,20 +141,21 @@ def build_cli() -> Path:
     return exe
 
 
-def build_oracle(with_reference: bool | None = None) -> None:
+def build_oracle(ref_root: str | None = None) -> None:
     """CPU oracle (test infrastructure): oracle/liboracle.so, plus the
-    reference harness oracle/_ref/libref.so when the reference sources exist."""
+    reference harness oracle/_ref/libref.so when ref_root (default: the
+    SSPMV_REF_ROOT environment variable) names a checkout of the reference
+    sources."""
     od = ROOT / "oracle"
     subprocess.run(["make", "-s", "-C", str(od)], check=True)
-    ref_root = os.environ.get("SSPMV_REF_ROOT", "/root/reference")
-    if with_reference is None:
-        with_reference = Path(ref_root, "LeSpMV", "include").is_dir()
-    if with_reference:
+    ref_root = ref_root or os.environ.get("SSPMV_REF_ROOT")
+    if ref_root and Path(ref_root, "LeSpMV", "include").is_dir():
         subprocess.run(["make", "-s", "-C", str(od), "ref", f"REF_ROOT={ref_root}"], check=True)
 
 
 if __name__ == "__main__":
     print(build_library(verbose=True))
     print(build_synth())
+    print(build_probe())
     print(build_cli())
     build_oracle()

@@ -109,6 +109,19 @@ extern "C" const char *sspmv_version(void) { return "sspmv-gb300 0.1 (sm_103a)";
 
 extern "C" int64_t sspmv_launch_count(void) { return (int64_t)g_launches.load(); }
 
+extern "C" sspmv_status sspmv_release_plan(sspmv_features *f, sspmv_stream_t s) {
+    if (!f) return fail(SSPMV_INVALID_ARG, "null matrix");
+    int param = 0;
+    if (f->priv) param = reinterpret_cast<Plan *>(f->priv)->param;
+    free_plan(f, s);  // f->kernel_flag stays
+    if (param != 0) {  // keep the kernel parameter (a host-side record; no device memory)
+        Plan *p = get_plan(f);
+        if (!p) return fail(SSPMV_OUT_OF_MEMORY, "plan allocation failed");
+        p->param = param;
+    }
+    return SSPMV_OK;
+}
+
 extern "C" sspmv_status sspmv_set_kernel(sspmv_features *f, int32_t kernel_flag, int32_t param) {
     if (!f) return fail(SSPMV_INVALID_ARG, "null matrix");
     if (kernel_flag < 0 || param < 0) return fail(SSPMV_INVALID_ARG, "negative kernel_flag or param");

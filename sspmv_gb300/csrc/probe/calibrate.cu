@@ -1,6 +1,10 @@
 // calibrate.cu -- measured ceilings the SpMV kernels are set against: random
 // gathers from the x vector, and FP64 FMA throughput.
 //
+// Measurement probes of the benchmark, not part of the SpMV library: built
+// on their own into lib/libsspmv_probe.so (linked against libsspmv.so) and
+// loaded only by the benchmark and its tests.
+//
 // SpMV on matrices whose column indices are spread at random (uniform,
 // power-law) is bound by the x gathers, not by HBM: every gathered element
 // costs one L1 line lookup (a warp's gather touches 32 distinct lines) and

@@ -18,6 +18,8 @@
 //
 // kernel_flag 1: vector-per-row kernel, `lanes` threads per row (2..32,
 // chosen from the mean row length, or set by the autotuner).
+#include <cuda.h>
+#include <mutex>
 #include <type_traits>
 
 #include "common.cuh"
@@ -1636,7 +1638,8 @@ extern "C" double sspmv_algorithmic_bytes_csr(const sspmv_csr *A, int32_t k, int
 //    million); larger matrices get SSPMV_INVALID_ARG.
 //  - the first call on a device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture.
+//    before any stream capture.  The address is kept per device and per
+//    context: after a cudaDeviceReset the next call looks it up again.
 //  - every call writes all the scratch it later reads (split points, carries),
 //    so nothing has to be cleared between calls; but all calls share the one
 //    array: calls that overlap on the GPU (different streams, or a graph
@@ -1655,18 +1658,52 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mutex;
 void *g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
+unsigned long long g_noalloc_ctx[kNoAllocMaxDevices] = {0};
 
+// Unique id of the calling thread's current CUDA context (0 if the driver
+// cannot tell), through the driver entry points the runtime hands out, so
+// no link against the driver library is needed.  A device reset
+// (cudaDeviceReset) ends the primary context and the next call gets a new
+// one with a new id: the array's address is then looked up again.
+unsigned long long current_context_id() {
+    using GetCurrent = CUresult (*)(CUcontext *);
+    using GetId = CUresult (*)(CUcontext, unsigned long long *);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(f);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(f);
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current && get_id && get_current(&ctx) == CUDA_SUCCESS && ctx && get_id(ctx, &id) == CUDA_SUCCESS)
+        return id;
+    return 0;
+}
+
+// The scratch array's device address on the current device, looked up with
+// cudaGetSymbolAddress the first time this device (context) is seen.
 sspmv_status noalloc_scratch(void **out) {
     int dev = 0;
     SSPMV_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(SSPMV_NOT_SUPPORTED, "device ordinal %d too large", dev);
+    SSPMV_CUDA_TRY(cudaSetDevice(dev));  // makes the device's primary context current (allocates nothing)
+    const unsigned long long ctx = current_context_id();
     std::lock_guard<std::mutex> g(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
+    if (!g_noalloc_ptr[dev] || g_noalloc_ctx[dev] != ctx || ctx == 0) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p)
             return fail(SSPMV_CUDA_ERROR, "cudaGetSymbolAddress(scratch) on device %d: %s", dev, cudaGetErrorString(e));
         g_noalloc_ptr[dev] = p;
+        g_noalloc_ctx[dev] = ctx;
     }
     *out = g_noalloc_ptr[dev];
     return SSPMV_OK;

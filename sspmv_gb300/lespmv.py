@@ -348,24 +348,6 @@ def grx_features(csr: CSR_Matrix, tile_blocks: int = 256, group: int = 0, stream
     return out
 
 
-def gather_ceiling(dtype, num_cols: int, num_gathers: int, stream=None) -> tuple[float, float]:
-    """Measured random-gather rate (gathers/s) from a vector of num_cols
-    values, the bound of SpMV on matrices with random column indices, and the
-    kernel's checksum (sum of its per-thread sums)."""
-    rate, chk = C.c_double(0.0), C.c_double(0.0)
-    call("sspmv_gather_ceiling", _vt(dtype), int(num_cols), int(num_gathers), C.byref(rate), C.byref(chk),
-         _stream(stream))
-    return rate.value, chk.value
-
-
-def fp64_ceiling(stream=None) -> float:
-    """Measured FP64 FMA rate of the device (FMAs/s), the bound of FP64 SpMV
-    where neither bytes nor gathers bind (one FMA per nonzero)."""
-    rate = C.c_double(0.0)
-    call("sspmv_fp64_ceiling", C.byref(rate), _stream(stream))
-    return rate.value
-
-
 def wait_timeouts() -> int:
     """Bounded device waits that gave up since the library was loaded (0 in
     every correct run)."""

@@ -65,20 +65,16 @@ def test_cli_runs_and_appends_reference_line(tmp_path, fmt, precision):
     assert re.match(LINES[fmt], line.rstrip("\n")), repr(line)
 
 
-def test_profile_case_usage():
-    """The one-case profiling driver parses its arguments without a GPU."""
+def test_bench_selects_one_case():
+    """One case of the benchmark (the profiling command of profiles/) is
+    selected by arguments alone: family, format, precision, sections."""
     import sys
-    r = subprocess.run([sys.executable, "-m", "sspmv_gb300.profile_case", "--help"], capture_output=True, text=True)
-    assert r.returncode == 0 and "family" in r.stdout
-    r = subprocess.run([sys.executable, "-m", "sspmv_gb300.profile_case", "powerlaw_4M", "nosuchformat", "f64"],
-                       capture_output=True, text=True)
-    assert r.returncode != 0
-
-
-@pytest.mark.gpu
-def test_profile_case_runs():
-    import sys
-    r = subprocess.run([sys.executable, "-m", "sspmv_gb300.profile_case", "banded_2M", "csr", "f32", "--reps", "1"],
-                       capture_output=True, text=True, timeout=600)
-    assert r.returncode == 0, r.stderr
-    assert "banded_2M csr f32 ms" in r.stdout
+    from pathlib import Path
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    import bench
+    a = bench.parse_args(["--families", "banded_2M", "--formats", "csr", "--dtypes", "f32", "--steps", "1",
+                          "--warmup", "3", "--sections", "suite", "--no-cpu", "--no-e2e"])
+    assert (a.families, a.formats, a.dtypes, a.steps) == ("banded_2M", "csr", "f32", 1)
+    assert bench.sections(a) == {"suite"}
+    assert bench.sections(bench.parse_args([])) == {"suite", "laplacian", "large", "serving"}
+    assert bench.sections(bench.parse_args(["--no-serving", "--no-large"])) == {"suite"}

@@ -166,26 +166,3 @@ def test_csr_deterministic():
         LeSpMV_csr(1.0, M, x, 0.0, y)
         outs.append(to_host(y))
     assert all(np.array_equal(outs[0], o) for o in outs[1:])
-
-
-@pytest.mark.parametrize("dt", [np.float64, np.float32])
-def test_gather_ceiling_checksum(dt):
-    """The gather-ceiling kernel gathers x[h(i) mod n] for a splitmix64 mix h
-    of i: its checksum equals the same sum taken on the host."""
-    from sspmv_gb300.lespmv import gather_ceiling
-    n, count = 1000, 256 * 4000
-    rate, chk = gather_ceiling(dt, n, count)
-    z = np.arange(count, dtype=np.uint64) + np.uint64(12345) + np.uint64(0x9E3779B97F4A7C15)
-    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
-    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
-    z ^= z >> np.uint64(31)
-    idx = (z % np.uint64(n)).astype(np.int64)
-    x = (1.0 + (np.arange(n) % 7) * 0.125).astype(dt)
-    ref = float(x[idx].astype(np.float64).sum())
-    assert rate > 0
-    assert abs(chk - ref) <= 1e-6 * ref
-
-
-def test_fp64_ceiling_positive():
-    from sspmv_gb300.lespmv import fp64_ceiling
-    assert fp64_ceiling() > 1e9

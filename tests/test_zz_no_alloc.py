@@ -7,11 +7,11 @@ a latency-bound loop that cannot take cudaMalloc's implicit synchronisation,
 a component held to a device-memory budget enforced outside this library.
 Instead of a per-matrix plan it uses one fixed device array for its scratch.
 
-Checked here: on two calls in a row its output matches the regular entry
-point (sspmv_LeSpMV_csr) within the per-row bound the other GPU tests use,
-8*nnz_i*eps*|alpha|*sum_j|a_ij x_j| + 2*eps*|beta*y0_i|; it builds no plan
-on the matrix; and a matrix past its size limit is refused with
-SSPMV_INVALID_ARG before anything runs.  This file is collected last, and
+Checked here: on two calls in a row its output matches the FP64 oracle and
+the regular entry point (sspmv_LeSpMV_csr) within the per-row bound the
+other GPU tests use, 8*nnz_i*eps*|alpha|*sum_j|a_ij x_j| + 2*eps*|beta*y0_i|;
+it builds no plan on the matrix; and a matrix past its size limit is refused
+with SSPMV_INVALID_ARG before anything runs.  This file is collected last, and
 passes alone in a fresh process as well as after the other tests."""
 import ctypes as C
 
@@ -37,16 +37,19 @@ def test_noalloc_matches_regular_entry_point(dt, oracle_lib):
     from sspmv_gb300 import lespmv as L
 
     A = synth.generate(synth.powerlaw(300000, 1.8, 16.0, 40000, 0.02), 4, dt)
-    x = torch.from_numpy(synth.vector(A.num_cols, 0, dt)).cuda()
+    xh = synth.vector(A.num_cols, 0, dt)
+    x = torch.from_numpy(xh).cuda()
     y0 = synth.vector(A.num_rows, 3, dt)
     nnz_row = np.diff(A.row_offset)
-    _, absum = oracle_lib.spmm_ref(A, synth.vector(A.num_cols, 0, dt), 0.8, 0.7, y0)
+    y64, absum = oracle_lib.spmm_ref(A, xh, 0.8, 0.7, y0)  # FP64 oracle on the same inputs
 
     regular = L.csr_from_host(A)
     y_reg = torch.from_numpy(y0.copy()).cuda()
     L.LeSpMV(0.8, regular, x, 0.7, y_reg)
     torch.cuda.synchronize()
-    ref = y_reg.cpu().numpy().astype(np.float64)
+    ref = y_reg.cpu().numpy()
+    ok, mx, _ = tolerance_ok(ref, y64, absum, nnz_row, dt, 0.8, 0.7, y0)
+    assert ok, f"regular entry point: max normalised error {mx}"
 
     M = L.csr_from_host(A)  # a fresh matrix: the no-alloc call must not give it a plan
     for call in range(2):
@@ -54,8 +57,13 @@ def test_noalloc_matches_regular_entry_point(dt, oracle_lib):
         st = _noalloc(0.8, M, x, 0.7, y)
         assert st == 0, _lib.lib.sspmv_last_error().decode()
         torch.cuda.synchronize()
-        ok, mx, _ = tolerance_ok(y.cpu().numpy(), ref, absum, nnz_row, dt, 0.8, 0.7, y0)
-        assert ok, f"call {call + 1}: max normalised error {mx}"
+        yg = y.cpu().numpy()
+        ok, mx, _ = tolerance_ok(yg, y64, absum, nnz_row, dt, 0.8, 0.7, y0)
+        assert ok, f"call {call + 1}: max normalised error {mx} against the FP64 oracle"
+        # and against the existing entry point's output, the same bound with
+        # that output in the reference's place
+        ok, mx, _ = tolerance_ok(yg, ref.astype(np.float64), absum, nnz_row, dt, 0.8, 0.7, y0)
+        assert ok, f"call {call + 1}: max normalised error {mx} against sspmv_LeSpMV_csr"
     assert not M.s.f.priv, "the allocation-free entry point built a plan"
 
 
@@ -78,9 +86,10 @@ def test_noalloc_rejects_matrices_past_its_limit():
 
 @pytest.mark.gpu
 def test_torch_custom_op_matches_library_call():
-    """torch.ops.sspmv.spmv_csr (stateless, on the no-allocation entry point)
-    equals sspmv_LeSpMV_csr with the merge-path kernel bit for bit, 1-D and
-    2-D x."""
+    """torch.ops.sspmv.spmv_csr (stateless: 1-D x on the no-allocation entry
+    point, 2-D x on the library's SpMM with its plan released after the call)
+    equals sspmv_LeSpMV_csr with the merge-path kernel bit for bit, and
+    rejects CPU tensors and mismatched lengths before any launch."""
     import torch
     import sspmv_gb300.torch_ops  # noqa: F401  (registers the operator)
     from sspmv_gb300 import synth
@@ -100,3 +109,7 @@ def test_torch_custom_op_matches_library_call():
             LeSpMV_csr(1.0, M, X[:, j].contiguous(), 0.0, ref)
             assert torch.equal(Y[:, j], ref)
         assert torch.equal(y1, Y[:, 1])
+    with pytest.raises(ValueError):
+        torch.ops.sspmv.spmv_csr(rp, ci, cv[:-1], A.num_cols, X[:, 0].contiguous())
+    with pytest.raises(ValueError):
+        torch.ops.sspmv.spmv_csr(rp.cpu(), ci, cv, A.num_cols, X[:, 0].contiguous())
