@@ -39,7 +39,7 @@ def feasible_host(fmt: str, A) -> tuple[bool, str]:
     if fmt == "bsr":
         r, c = bsr_block_for(A)
         rows = np.repeat(np.arange(m, dtype=np.int64), lens) // r
-        keys = rows * ((A.num_cols + c - 1) // c) + A.col_index // c
-        nnzb = len(np.unique(keys))
+        keys = np.sort(rows * ((A.num_cols + c - 1) // c) + A.col_index // c, kind="stable")  # radix sort
+        nnzb = int(keys.size > 0) + int(np.count_nonzero(keys[1:] != keys[:-1]))
         return (nnzb * r * c <= MAX_FILL * nnz, f"BSR {r}x{c} fill {nnzb * r * c / nnz:.1f}x")
     return False, "unknown format"
