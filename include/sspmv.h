@@ -219,7 +219,7 @@ int64_t sspmv_launch_count(void);
 sspmv_status sspmv_release_plan(sspmv_features *f, sspmv_stream_t stream);
 /* Selects the SpMV kernel of a matrix (pass &A->f): kernel_flag as in each
  * format's LeSpMV entry, param a kernel parameter (0 lets the library
- * choose): CSR vector kernel: lanes per row 2..32; CSR row-block kernel:
+ * choose): CSR vector kernel: lanes per row 1..32; CSR row-block kernel:
  * nonzeros per block window (512, 1024, 2048, 4096); S-ELL, SELL-c-sigma,
  * SELL-c-R: the slots a row's thread reads before the rest of the row moves
  * to the overflow CSR pass (default: a cost model over the row lengths).
@@ -252,7 +252,7 @@ sspmv_status sspmv_delete_csr(sspmv_csr *A);
 /* LeSpMV_csr (src/spmv_csr.cpp:165-185).  kernel_flag 0 (default):
  * nonzero-split stream kernel (256 nonzeros per warp; matrices with runs of
  * more than 256 empty rows use merge-path); 2: nnz-balanced merge-path
- * kernel; 1: vector-per-row kernel (param: lanes per row); 3: row-block
+ * kernel; 1: vector-per-row kernel (param: lanes per row, 1..32); 3: row-block
  * kernel for matrices whose rows all have at most 64 nonzeros (one CTA per
  * block of whole rows, param: nonzeros per block window, 512..4096; one
  * right-hand side; other matrices and k > 1 run the default kernel). */

@@ -7,7 +7,7 @@ fastest is kept.  Results are plain dicts, so a caller can store them as an
 append-only JSONL log keyed by matrix and re-apply them without re-measuring.
 
 CSR candidates: stream kernel (default), merge-path kernel, vector kernel with
-2..32 lanes per row, row-block kernel (short rows) with windows of 512..4096
+1..32 lanes per row, row-block kernel (short rows) with windows of 512..4096
 nonzeros.
 S-ELL / SELL-c-sigma / SELL-c-R: after the layout, the thread-pass cap (the
 cost model's choice against caps of 16..128 slots).
@@ -63,7 +63,7 @@ def time_spmv(M, x, y, reps: int = 10, warmup: int = 2, flush=None, stream=None)
     return ts[len(ts) // 2]
 
 
-CSR_CANDIDATES = ([(0, 0), (2, 0)] + [(1, vs) for vs in (2, 4, 8, 16, 32)] +
+CSR_CANDIDATES = ([(0, 0), (2, 0)] + [(1, vs) for vs in (1, 2, 4, 8, 16, 32)] +
                   [(3, w) for w in (512, 1024, 2048, 4096)])
 
 

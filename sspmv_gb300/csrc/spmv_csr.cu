@@ -261,6 +261,8 @@ __global__ void csr_merge_fixup(int64_t num_tiles, int m, const int32_t *__restr
     }
 }
 
+constexpr int kVecHoist = 6;
+
 template <typename V, int K, int VS, bool PLAIN = false>
 __global__ void __launch_bounds__(kBlock) csr_vector_kernel(
     int m, const int32_t *__restrict__ row_offset, const int32_t *__restrict__ col_index,
@@ -276,8 +278,42 @@ __global__ void __launch_bounds__(kBlock) csr_vector_kernel(
         V s[K];
 #pragma unroll
         for (int r = 0; r < K; r++) s[r] = V(0);
+        int rs = 0, re = 0;
         if (row < m) {
-            const int rs = ld_stream(row_offset + row), re = ld_stream(row_offset + row + 1);
+            rs = ld_stream(row_offset + row);
+            re = ld_stream(row_offset + row + 1);
+        }
+        // One lane per row, short rows (every lane of the warp with at most
+        // kVecHoist elements): all of a lane's column and value loads, then
+        // all its x gathers, are issued before its first FMA -- one memory
+        // round trip each instead of one per element (same summation order
+        // as the loop).  Measured: FP32 5-point Laplacian 22 -> 17 us; with
+        // 2+ lanes per row the loop below was faster.
+        const int cnt = re - rs > sub ? (re - rs - sub + VS - 1) / VS : 0;
+        const int wmax = (VS == 1 && K <= 2) ? __reduce_max_sync(0xffffffffu, cnt) : kVecHoist + 1;
+        if (wmax <= kVecHoist) {
+            int c[kVecHoist];
+            V a[kVecHoist];
+#pragma unroll
+            for (int q = 0; q < kVecHoist; q++) {
+                c[q] = 0;  // a lane past its elements gathers x row 0 (exists: some lane has elements) with value 0
+                a[q] = V(0);
+                if (q < cnt) {
+                    c[q] = ld_stream(col_index + rs + sub + q * VS);
+                    a[q] = ld_stream(values + rs + sub + q * VS);
+                }
+            }
+            V xr[kVecHoist][K];
+#pragma unroll
+            for (int q = 0; q < kVecHoist; q++)
+                if (q < wmax) ld_xrow<V, K>(x, c[q], ldx, xvec != 0, xr[q]);
+#pragma unroll
+            for (int q = 0; q < kVecHoist; q++)
+                if (q < cnt) {  // never 0 * x[0]: x may hold Inf or NaN
+#pragma unroll
+                    for (int r = 0; r < K; r++) s[r] += a[q] * xr[q][r];
+                }
+        } else if (row < m) {
             int j = rs + sub;
             for (; j + 3 * VS < re; j += 4 * VS) {  // four independent gathers in flight
                 int c[4];
@@ -366,6 +402,7 @@ sspmv_status launch_vector(const sspmv_csr *A, Plan *p, V alpha, const V *x, int
         while (vs < 32 && vs < mean) vs <<= 1;
     }
     switch (vs) {
+    case 1: return launch_vector_vs<V, K, 1>(A, alpha, x, ldx, beta, y, ldy, s);
     case 2: return launch_vector_vs<V, K, 2>(A, alpha, x, ldx, beta, y, ldy, s);
     case 4: return launch_vector_vs<V, K, 4>(A, alpha, x, ldx, beta, y, ldy, s);
     case 8: return launch_vector_vs<V, K, 8>(A, alpha, x, ldx, beta, y, ldy, s);
