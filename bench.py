@@ -357,8 +357,10 @@ def run_suite(args, dev, rank, world):
     sampler.start()
     launches0 = _lib.lib.sspmv_launch_count()
     t0 = time.perf_counter()
+    torch.cuda.nvtx.range_push("timed_steps")  # profilers select the timed launches by this range
     for _ in range(args.steps):
         one_step(rec)
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     launches = _lib.lib.sspmv_launch_count() - launches0
