@@ -98,9 +98,16 @@ struct Request {
     void *d_x = nullptr, *d_y = nullptr;
 };
 
+// Requests of a batch that are not in the batched CSR launch (other formats,
+// other k) run on up to kAuxStreams streams of their workspace at once,
+// forked from and joined back into the workspace stream.
+constexpr int kAuxStreams = 4;
+
 struct Workspace {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
+    cudaStream_t aux[kAuxStreams] = {nullptr};
+    cudaEvent_t fork = nullptr, join[kAuxStreams] = {nullptr};
     unsigned char *h_in = nullptr, *d_in = nullptr, *h_out = nullptr, *d_out = nullptr;
     void *carry = nullptr;
     cudaGraphExec_t graph = nullptr;  // all groups' batch kernels (ensure_graph)
@@ -242,6 +249,11 @@ sspmv_status Server::init() {
     for (auto &w : ws) {
         SSPMV_CUDA_TRY(cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking));
         SSPMV_CUDA_TRY(cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming));
+        SSPMV_CUDA_TRY(cudaEventCreateWithFlags(&w.fork, cudaEventDisableTiming));
+        for (int a = 0; a < kAuxStreams; a++) {
+            SSPMV_CUDA_TRY(cudaStreamCreateWithFlags(&w.aux[a], cudaStreamNonBlocking));
+            SSPMV_CUDA_TRY(cudaEventCreateWithFlags(&w.join[a], cudaEventDisableTiming));
+        }
         SSPMV_CUDA_TRY(cudaMalloc(&w.d_in, in_bytes));
         SSPMV_CUDA_TRY(cudaMalloc(&w.d_out, out_bytes));
         SSPMV_CUDA_TRY(cudaMallocHost(&w.h_in, in_bytes));
@@ -284,6 +296,14 @@ void Server::shutdown() {
         cudaFreeHost(w.h_out);
         cudaFree(w.carry);
         if (w.done) cudaEventDestroy(w.done);
+        for (int a = 0; a < kAuxStreams; a++) {
+            if (w.aux[a]) {
+                cudaStreamSynchronize(w.aux[a]);
+                cudaStreamDestroy(w.aux[a]);
+            }
+            if (w.join[a]) cudaEventDestroy(w.join[a]);
+        }
+        if (w.fork) cudaEventDestroy(w.fork);
         if (w.stream) cudaStreamDestroy(w.stream);
     }
     if (load_stream) {
@@ -633,17 +653,40 @@ void Server::issue(Batch &b) {
     }
     sspmv_status st = SSPMV_OK;
     if (e == cudaSuccess && mask) st = launch_groups(w, mask);
-    sspmv_stream_t s = reinterpret_cast<sspmv_stream_t>(w.stream);
+    // Own launches: with more than one, spread over the auxiliary streams
+    // (forked after the copies in), so independent requests overlap on the
+    // GPU; launches on one matrix stay ordered through its event.
+    int own = 0;
+    for (Request *r : b.reqs)
+        if (r->group < 0 && r->mat->m > 0) own++;
+    bool used[kAuxStreams] = {false};
+    if (own > 1 && e == cudaSuccess) e = cudaEventRecord(w.fork, w.stream);
+    int j = 0;
     for (Request *r : b.reqs) {
         if (e != cudaSuccess || st != SSPMV_OK) break;
         if (r->group >= 0) continue;
         Matrix &M = *r->mat;
         if (M.m == 0) continue;
-        if (M.ev_stream && M.ev_stream != w.stream) cudaStreamWaitEvent(w.stream, M.ev, 0);
-        st = spmm(M, r->r.alpha, r->r.k, r->d_x, r->r.ldx, r->r.beta, r->d_y, r->r.ldy, s);
-        cudaEventRecord(M.ev, w.stream);
-        M.ev_stream = w.stream;
+        cudaStream_t cs = w.stream;
+        if (own > 1) {
+            const int a = j++ % kAuxStreams;
+            cs = w.aux[a];
+            if (!used[a]) {
+                cudaStreamWaitEvent(cs, w.fork, 0);
+                used[a] = true;
+            }
+        }
+        if (M.ev_stream && M.ev_stream != cs) cudaStreamWaitEvent(cs, M.ev, 0);
+        st = spmm(M, r->r.alpha, r->r.k, r->d_x, r->r.ldx, r->r.beta, r->d_y, r->r.ldy,
+                  reinterpret_cast<sspmv_stream_t>(cs));
+        cudaEventRecord(M.ev, cs);
+        M.ev_stream = cs;
     }
+    for (int a = 0; a < kAuxStreams; a++)
+        if (used[a]) {
+            cudaEventRecord(w.join[a], w.aux[a]);
+            cudaStreamWaitEvent(w.stream, w.join[a], 0);
+        }
     if (e == cudaSuccess && st == SSPMV_OK && b.staged_y_bytes)
         e = cudaMemcpyAsync(w.h_out, w.d_out, b.staged_y_bytes, cudaMemcpyDeviceToHost, w.stream);
     for (Request *r : b.reqs) {

@@ -326,23 +326,69 @@ def _us(v) -> str:
     return "n/a" if v is None else f"{v:.0f} us"
 
 
-def serving_benchmark(num_matrices: int = 64, device_buffers: bool = False, duration_s: float = 1.5,
-                      seed: int = 0, log=None, selector_model=None) -> dict:
+SWEEP_FRACTIONS = (0.2, 0.4, 0.6, 0.8, 1.0, 1.2, 1.5)
+
+
+def throughput_at_p99(sweep: list[dict], target_us: float) -> float | None:
+    """Highest completed-request throughput at which a server's p99 stays
+    within target_us, linearly interpolated between its sweep points (p99 as
+    a function of throughput, points in offered-rate order).  None if even
+    its lightest point is above the target."""
+    pts = [(r["req_per_s"], r["p99_us"]) for r in sweep if r.get("p99_us") is not None]
+    if not pts or pts[0][1] > target_us:
+        return None
+    best = pts[0][0]
+    for (t0, p0), (t1, p1) in zip(pts, pts[1:]):
+        if p1 <= target_us:
+            best = max(best, t1)
+            continue
+        if p0 <= target_us < p1 and p1 > p0:  # crosses the target between these points
+            best = max(best, t0 + (t1 - t0) * (target_us - p0) / (p1 - p0))
+        break
+    return best
+
+
+def equal_p99(res: dict, batched: str = "batched") -> dict:
+    """Throughput of the batched server against each baseline at equal p99.
+    The target is the baseline's p99 at its most loaded sweep point that
+    still keeps up with the offered rate (completed >= 95% of offered); both
+    servers' throughputs at that p99 are interpolated from their sweeps."""
+    out = {}
+    bsw = res["modes"][batched]["sweep"]
+    for base in res["modes"]:
+        if base == batched:
+            continue
+        sw = res["modes"][base]["sweep"]
+        kept = [r for r in sw if r["offered_per_s"] and r["req_per_s"] >= 0.95 * r["offered_per_s"]]
+        if not kept:
+            continue
+        ref = kept[-1]
+        target = ref["p99_us"]
+        tb, tr = throughput_at_p99(bsw, target), throughput_at_p99(sw, target)
+        out[base] = {"p99_target_us": target, "baseline_req_per_s": tr, "batched_req_per_s": tb,
+                     "throughput_ratio": (tb / tr) if (tb and tr) else None}
+    return out
+
+
+def serving_benchmark(num_matrices: int = 64, device_buffers: bool = False, duration_s: float = 2.0,
+                      seed: int = 0, log=None, selector_model=None, fractions=SWEEP_FRACTIONS) -> dict:
     """Saturation throughput of the batched server and of per-request CSR
-    launches (8 requests in flight, and 1: the plain serial loop), then
-    p50/p99 under Poisson load swept up to saturation.  'Equal p99' takes a
-    baseline's most loaded sweep point and the batched server's best
-    throughput whose p99 is no higher."""
+    launches (8 requests in flight, and 1: the plain serial loop), then every
+    server under the same Poisson offered rates -- `fractions` of the 8-deep
+    per-request server's saturation, duration_s of arrivals per point (a
+    server is not run at rates above 1.2x its own saturation, where its queue
+    only grows) -- with p50/p99 per point, and the throughput ratios at
+    saturation and at equal p99 (interpolated)."""
     log = log or (lambda *a: None)
     b = ServingBench(num_matrices, seed, device_buffers, log)
     picks = select_formats(b.mats, selector_model, log=log) if selector_model else None
     res = {"matrices": num_matrices, "registered": 2 * num_matrices, "total_nnz_per_precision": b.total_nnz,
-           "buffers": "device" if device_buffers else "pinned host", "modes": {},
+           "buffers": "device" if device_buffers else "pinned host", "seconds_per_point": duration_s,
+           "modes": {},
            "server_config": {"per_request": {"num_inflight": 8, "arena_bytes": 160 << 20},
                              "per_request_serial": {"num_inflight": 1, "arena_bytes": 160 << 20},
                              "batched": {"num_inflight": 4, "arena_bytes": 512 << 20,
                                          "max_batch_tiles": 1 << 16}}}
-    # Per-request launches get more requests in flight (they cannot batch).
     server_kw = res["server_config"]
     if picks:
         res["formats"] = {f"{d['family']}:{d['n']}": pk[0] for d, pk in zip(b.mats, picks) if pk[0] != "csr"}
@@ -354,53 +400,72 @@ def serving_benchmark(num_matrices: int = 64, device_buffers: bool = False, dura
             return None
         return lambda mid, A: picks[mid // 2]
 
-    for mode in ("per_request_serial", "per_request", "batched"):
-        s = b.server("batched" if mode == "batched" else "per_request", fmt_of(mode), **server_kw[mode])
-        try:
+    modes = ("per_request", "per_request_serial", "batched")
+    servers = {}
+    try:
+        for mode in modes:
+            s = b.server("batched" if mode == "batched" else "per_request", fmt_of(mode), **server_kw[mode])
+            servers[mode] = s
             b.run(s, 2000, 0.0, seed + 1)  # warm: graphs for the group sets, pools
             sat = b.run(s, {"batched": 20000, "per_request": 8000, "per_request_serial": 3000}[mode], 0.0, seed + 2)
             log(f"[serving] {mode}: saturation {sat['req_per_s']:.0f} req/s, mean batch {sat['mean_batch']:.1f}")
             res["modes"][mode] = {"saturation": sat, "sweep": [], "stats": None}
-            res["modes"][mode]["_server"] = s
-        except Exception:
-            s.close()
-            raise
-    base = res["modes"]["per_request"]["saturation"]["req_per_s"]
-    fracs = {"per_request_serial": (0.1, 0.2, 0.3), "per_request": (0.3, 0.5, 0.7, 0.9),
-             "batched": (0.3, 0.7, 1.0, 1.5, 2.0, 3.0, 4.0, 6.0, 8.0)}
-    try:
-        for mode in ("per_request_serial", "per_request", "batched"):
+        base = res["modes"]["per_request"]["saturation"]["req_per_s"]
+        res["offered_rates_per_s"] = [f * base for f in fractions]
+        for mode in modes:
             m = res["modes"][mode]
             satm = m["saturation"]["req_per_s"]
-            for f in fracs[mode]:
+            for f in fractions:
                 rate = f * base
-                if rate > 1.05 * satm:
-                    break
-                n = int(min(max(rate * duration_s, 1000), 200000))
-                r = b.run(m["_server"], n, rate, seed + 10 + int(f * 100))
+                if rate > 1.2 * satm:
+                    m.setdefault("not_run_above_saturation", []).append(f)
+                    continue
+                n = int(min(max(rate * duration_s, 1000), 400000))
+                r = b.run(servers[mode], n, rate, seed + 10 + int(f * 100))
                 r["fraction_of_per_request_saturation"] = f
                 m["sweep"].append(r)
                 log(f"[serving] {mode} @ {rate:.0f}/s: {r['req_per_s']:.0f} req/s p50 {_us(r['p50_us'])} "
                     f"p99 {_us(r['p99_us'])} batch {r['mean_batch']:.1f} failed {r['failed']}")
-            m["stats"] = m["_server"].stats()
+            m["stats"] = servers[mode].stats()
     finally:
-        for mode in res["modes"].values():
-            mode.pop("_server").close()
-    # throughput at equal p99: the baseline's most loaded sweep point whose
-    # p99 is the target, against the batched server's best throughput within it
+        for s in servers.values():
+            s.close()
     res["saturation_ratio"] = {m: res["modes"]["batched"]["saturation"]["req_per_s"] /
                                max(res["modes"][m]["saturation"]["req_per_s"], 1e-9)
                                for m in ("per_request", "per_request_serial")}
-    res["equal_p99"] = {}
-    for base_mode in ("per_request", "per_request_serial"):
-        sw = res["modes"][base_mode]["sweep"]
-        if not sw:
-            continue
-        ref = sw[-1]
-        target = ref["p99_us"]
-        ok = [r for r in res["modes"]["batched"]["sweep"] if r["p99_us"] is not None and r["p99_us"] <= target]
-        best = max((r["req_per_s"] for r in ok), default=None)
-        res["equal_p99"][base_mode] = {"p99_target_us": target, "baseline_req_per_s": ref["req_per_s"],
-                                       "batched_req_per_s": best,
-                                       "throughput_ratio": (best / ref["req_per_s"]) if best else None}
+    res["equal_p99"] = equal_p99(res)
     return res
+
+
+def main(argv=None) -> None:
+    """python -m sspmv_gb300.serving sweep [--seconds 5] [--buffers device,host] [--out FILE]
+
+    The serving workload's full sweep (longer points than the benchmark's
+    default run), one JSON document per buffer kind."""
+    import argparse
+    import json
+    import sys
+    from pathlib import Path
+    ap = argparse.ArgumentParser(prog="python -m sspmv_gb300.serving")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    sw = sub.add_parser("sweep")
+    sw.add_argument("--seconds", type=float, default=5.0)
+    sw.add_argument("--buffers", default="device,host")
+    sw.add_argument("--matrices", type=int, default=64)
+    sw.add_argument("--out", default="")
+    a = ap.parse_args(argv)
+    model = Path(__file__).resolve().parent / "data" / "selector_model.npz"
+    out = {}
+    for kind in a.buffers.split(","):
+        out[kind] = serving_benchmark(a.matrices, device_buffers=(kind == "device"), duration_s=a.seconds,
+                                      log=lambda m: print(m, file=sys.stderr, flush=True),
+                                      selector_model=model if model.exists() else None)
+    text = json.dumps(out, indent=1)
+    if a.out:
+        Path(a.out).write_text(text)
+    summary = {k: {"saturation_ratio": v["saturation_ratio"], "equal_p99": v["equal_p99"]} for k, v in out.items()}
+    print(json.dumps(summary))
+
+
+if __name__ == "__main__":
+    main()

@@ -57,3 +57,29 @@ def test_latency_summary():
     assert abs(s["p50_us"] - 50.0) < 1.0 and s["p99_us"] <= 99.0
     assert s["mean_batch"] == 4.0
 
+
+
+def test_throughput_at_p99_interpolates():
+    from sspmv_gb300.serving import throughput_at_p99
+    sw = [{"req_per_s": 1000.0, "p99_us": 100.0}, {"req_per_s": 2000.0, "p99_us": 200.0},
+          {"req_per_s": 2900.0, "p99_us": 1000.0}]
+    assert throughput_at_p99(sw, 150.0) == 1500.0   # halfway between the first two points
+    assert throughput_at_p99(sw, 600.0) == 2450.0
+    assert throughput_at_p99(sw, 5000.0) == 2900.0  # every point within the target
+    assert throughput_at_p99(sw, 50.0) is None      # even the lightest point is above it
+
+
+def test_equal_p99_uses_the_baselines_last_sustained_point():
+    from sspmv_gb300.serving import equal_p99
+
+    def pt(off, got, p99):
+        return {"offered_per_s": off, "req_per_s": got, "p99_us": p99}
+    res = {"modes": {
+        "batched": {"sweep": [pt(1000, 1000, 50), pt(2000, 2000, 60), pt(3000, 3000, 80), pt(4000, 3990, 400)]},
+        "per_request": {"sweep": [pt(1000, 1000, 100), pt(2000, 1990, 300), pt(3000, 2500, 9000)]},
+    }}
+    eq = equal_p99(res)["per_request"]
+    assert eq["p99_target_us"] == 300            # 3000 offered, 2500 done: not sustained
+    assert eq["baseline_req_per_s"] == 1990
+    assert abs(eq["batched_req_per_s"] - (3000 + 990 * 220 / 320)) < 1e-6
+    assert abs(eq["throughput_ratio"] - eq["batched_req_per_s"] / 1990) < 1e-12
