@@ -437,11 +437,67 @@ def serving_benchmark(num_matrices: int = 64, device_buffers: bool = False, dura
     return res
 
 
+def mix_bound(num_matrices: int = 64, seed: int = 0, thresholds=(1e5, 1e6, 4e6), log=None) -> dict:
+    """GPU time per request of the serving mix, request kind by request kind
+    (matrix x precision x k, each equally likely, as in request_stream): the
+    request's CSR SpMM captured 20 times in a CUDA graph, replayed, timed
+    with CUDA events (no host launch gaps; warm).  Reports the mean, and the
+    share of it spent on requests whose matrix has at least each threshold
+    of nonzeros: work that batching cannot remove, which bounds any
+    server's throughput at about 1 / (that share)."""
+    import torch
+    from . import lespmv as L
+    mats = serving_matrices(num_matrices, seed=seed)
+    recs = []
+    for i, d in enumerate(mats):
+        for dt in (np.float64, np.float32):
+            A = d["A"] if dt == np.float64 else d["A"].astype(np.float32)
+            csr = L.csr_from_host(A)
+            tdt = torch.float64 if dt == np.float64 else torch.float32
+            for k in (1, 2, 4, 8):
+                X = torch.rand((A.num_cols, k), dtype=tdt, device="cuda")
+                Y = torch.zeros((A.num_rows, k), dtype=tdt, device="cuda")
+                for _ in range(3):  # plans built before capture
+                    L.spmm(1.0, csr, X, 0.0, Y)
+                torch.cuda.synchronize()
+                g = torch.cuda.CUDAGraph()
+                st = torch.cuda.Stream()
+                with torch.cuda.stream(st):
+                    with torch.cuda.graph(g, stream=st):
+                        for _ in range(20):
+                            L.spmm(1.0, csr, X, 0.0, Y)
+                g.replay()
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                g.replay()
+                e1.record()
+                e1.synchronize()
+                recs.append({"matrix": i, "nnz": A.nnz, "dtype": np.dtype(dt).name, "k": k,
+                             "us": e0.elapsed_time(e1) * 1e3 / 20})
+                del g, X, Y
+            csr.delete()
+        if log:
+            log(f"[serving bound] matrix {i}: nnz {d['A'].nnz}")
+    n = len(recs)
+    mean = sum(r["us"] for r in recs) / n
+    out = {"request_kinds": n, "mean_us_per_request": mean, "bound_req_per_s": 1e6 / mean, "split": []}
+    for t in thresholds:
+        big = sum(r["us"] for r in recs if r["nnz"] >= t) / n
+        out["split"].append({"nnz_at_least": t, "kinds": sum(1 for r in recs if r["nnz"] >= t),
+                             "mean_us_of_these": big, "mean_us_of_the_rest": mean - big,
+                             "bound_req_per_s_from_these": (1e6 / big) if big > 0 else None})
+    out["requests"] = recs
+    return out
+
+
 def main(argv=None) -> None:
     """python -m sspmv_gb300.serving sweep [--seconds 5] [--buffers device,host] [--out FILE]
+    python -m sspmv_gb300.serving bound [--out FILE]
 
-    The serving workload's full sweep (longer points than the benchmark's
-    default run), one JSON document per buffer kind."""
+    sweep: the serving workload's full sweep (longer points than the
+    benchmark's default run), one JSON document per buffer kind.
+    bound: GPU time per request of the mix (mix_bound)."""
     import argparse
     import json
     import sys
@@ -453,7 +509,16 @@ def main(argv=None) -> None:
     sw.add_argument("--buffers", default="device,host")
     sw.add_argument("--matrices", type=int, default=64)
     sw.add_argument("--out", default="")
+    bd = sub.add_parser("bound")
+    bd.add_argument("--matrices", type=int, default=64)
+    bd.add_argument("--out", default="")
     a = ap.parse_args(argv)
+    if a.cmd == "bound":
+        res = mix_bound(a.matrices, log=lambda m: print(m, file=sys.stderr, flush=True))
+        if a.out:
+            Path(a.out).write_text(json.dumps(res, indent=1))
+        print(json.dumps({k: v for k, v in res.items() if k != "requests"}))
+        return
     model = Path(__file__).resolve().parent / "data" / "selector_model.npz"
     out = {}
     for kind in a.buffers.split(","):
