@@ -398,11 +398,13 @@ def test_bsr_block_stream_shapes(dt, oracle_lib):
 @pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
 def test_plain_sum_instantiations(dt, oracle_lib):
     """alpha = 1, beta = 0 (y = sum, the kernels' multiply-free instantiation)
-    through the CSR stream / vector, COO warp, CSR5 tile, BSR and sliced
+    through the CSR stream / vector (one and several lanes per row) / row-block,
+    COO warp, CSR5 tile, BSR (block-stream and thread-per-row) and sliced
     (S-ELL, SELL-c-sigma, SELL-c-R, with their overflow passes) kernels, on
     rows that end at every position of a lane's nonzeros (power-law rows with
-    empty rows): within tolerance of the FP64 product, and y fully written
-    (a NaN-filled y comes back finite)."""
+    empty rows), and DIA and thread-per-row BSR on a banded matrix: within
+    tolerance of the FP64 product, and y fully written (a NaN-filled y comes
+    back finite)."""
     from sspmv_gb300 import lespmv as L
     from sspmv_gb300 import synth
     A = synth.generate(synth.powerlaw(20000, 1.7, 5.0, 3000, 0.2), 21, dt)
@@ -413,12 +415,21 @@ def test_plain_sum_instantiations(dt, oracle_lib):
     cases = [("csr0", M, 0), ("csr1", M, 1), ("csr3", M, 3), ("coo", L.csr_to_coo(M), 0),
              ("csr5", L.csr_to_csr5(M), 0), ("bsr", L.csr_to_bsr(M, 4, 4), 2),
              ("sell", L.csr_to_sell(M, 4, 0), 0), ("scs", L.csr_to_sell_c_sigma(M, 256, 8, 0), 0),
-             ("scr", L.csr_to_sell_c_R(M, 16, 0), 0)]
-    for name, G, flag in cases:
-        G.set_kernel(flag, 0)
-        Y = to_dev(np.full(A.num_rows, np.nan, dt))
-        L.LeSpMV(1.0, G, to_dev(x), 0.0, Y)
+             ("scr", L.csr_to_sell_c_R(M, 16, 0), 0), ("bsr1", L.csr_to_bsr(M, 4, 4), 1),
+             ("csr1_one_lane", M, (1, 1))]
+    # DIA needs few diagonals: a banded matrix (9 diagonals, ragged first and last rows)
+    B = synth.generate(synth.banded(30001), 22, dt)
+    MB = L.csr_from_host(B)
+    xb = synth.vector(B.num_cols, 0, dt)
+    yb64, absb = oracle_lib.spmm_ref(B, xb.reshape(-1, 1), 1.0, 0.0, None)
+    runs = [(name, G, flag, A, x, y64, absum, nnz_row) for name, G, flag in cases]
+    runs += [("dia", L.csr_to_dia(MB), 0, B, xb, yb64, absb, np.diff(B.row_offset)),
+             ("bsr1_banded", L.csr_to_bsr(MB, 4, 4), 1, B, xb, yb64, absb, np.diff(B.row_offset))]
+    for name, G, flag, H, xh, yr, ab, nr in runs:
+        G.set_kernel(*(flag if isinstance(flag, tuple) else (flag, 0)))
+        Y = to_dev(np.full(H.num_rows, np.nan, dt))
+        L.LeSpMV(1.0, G, to_dev(xh), 0.0, Y)
         y = to_host(Y)
         assert np.isfinite(y).all(), name
-        ok, mx, _ = tolerance_ok(y.reshape(-1, 1), y64, absum, nnz_row, dt, 1.0, 0.0, None)
+        ok, mx, _ = tolerance_ok(y.reshape(-1, 1), yr, ab, nr, dt, 1.0, 0.0, None)
         assert ok, f"{name}: max normalised error {mx}"
