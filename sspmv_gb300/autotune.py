@@ -44,7 +44,11 @@ class L2Flush:
 
 
 def time_spmv(M, x, y, reps: int = 10, warmup: int = 2, flush=None, stream=None) -> float:
-    """Median milliseconds of one SpMV (alpha=1, beta=0) with L2 flushed."""
+    """Milliseconds of one SpMV (alpha=1, beta=0) with L2 flushed: the mean
+    of the middle half of the sorted samples.  CUDA event times come in
+    steps of about 2 us on this GPU; the trimmed mean resolves kernels of
+    tens of microseconds better than the median, which can only take one of
+    those steps."""
     import torch
     stream = stream or torch.cuda.current_stream()
     if flush is None:
@@ -60,7 +64,9 @@ def time_spmv(M, x, y, reps: int = 10, warmup: int = 2, flush=None, stream=None)
         if i >= warmup:
             ts.append(e0.elapsed_time(e1))
     ts.sort()
-    return ts[len(ts) // 2]
+    q = len(ts) // 4
+    mid = ts[q:len(ts) - q] or ts
+    return sum(mid) / len(mid)
 
 
 CSR_CANDIDATES = ([(0, 0), (2, 0)] + [(1, vs) for vs in (1, 2, 4, 8, 16, 32)] +

@@ -1,6 +1,9 @@
 // calibrate.cu -- measured ceilings the SpMV kernels are set against: random
 // gathers from the x vector, and FP64 FMA throughput.
 //
+// A third probe times a plain stream of a given read and write volume, the
+// speed of light for a kernel of that size in the benchmark's cold-L2 timing.
+//
 // Measurement probes of the benchmark, not part of the SpMV library: built
 // on their own into lib/libsspmv_probe.so (linked against libsspmv.so) and
 // loaded only by the benchmark and its tests.
@@ -81,10 +84,91 @@ __global__ void __launch_bounds__(kBlockG) dfma_kernel(int64_t iters, double b, 
     out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// A size-matched stream: reads nr and writes nw 16-byte words of separate
+// buffers, grid-stride (consecutive threads, consecutive words), evict-first
+// loads; what DRAM delivers to a kernel of that size and shape.
+__global__ void __launch_bounds__(kBlockG) stream_kernel(const float4 *__restrict__ src, int64_t nr,
+                                                         float4 *__restrict__ dst, int64_t nw, float *__restrict__ sink) {
+    const int64_t n = nr > nw ? nr : nw;
+    float acc = 0.f;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 v = i < nr ? ld_stream(src + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (i < nw) dst[i] = v;
+        else acc += v.x + v.y + v.z + v.w;
+    }
+    if (acc == 1234.5f) *sink = acc;  // keeps the reads
+}
+
+__global__ void flush_read(const float4 *__restrict__ a, int64_t n, float *__restrict__ sink) {
+    float acc = 0.f;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 v = a[i];
+        acc += v.x + v.y + v.z + v.w;
+    }
+    if (acc == 1234.5f) *sink = acc;
+}
+
 }  // namespace
 }  // namespace sspmv
 
 using namespace sspmv;
+
+// Median time of the size-matched stream above, L2 flushed before every run
+// the way the benchmark flushes (256 MiB write, then 256 MiB read): the time
+// a kernel that only had to move read_bytes in and write_bytes out would
+// take, cold, at this size -- short kernels do not reach the bandwidth of a
+// multi-gigabyte copy.
+extern "C" sspmv_status sspmv_stream_ceiling(int64_t read_bytes, int64_t write_bytes, double *ms_out,
+                                             sspmv_stream_t stream) {
+    if (!ms_out || read_bytes < 0 || write_bytes < 0 || read_bytes + write_bytes <= 0)
+        return fail(SSPMV_INVALID_ARG, "stream ceiling: byte counts >= 0 (not both 0) and an output required");
+    const int64_t nr = (read_bytes + 15) / 16, nw = (write_bytes + 15) / 16;
+    const size_t kFlush = 256u << 20;
+    float4 *src = nullptr, *dst = nullptr, *fr = nullptr;
+    unsigned char *fw = nullptr;
+    float *sink = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    std::vector<float> ts;
+    auto body = [&]() -> sspmv_status {
+        SSPMV_TRY(dalloc(&src, (size_t)std::max<int64_t>(nr, 1), stream));
+        SSPMV_TRY(dalloc(&dst, (size_t)std::max<int64_t>(nw, 1), stream));
+        SSPMV_TRY(dalloc(&fr, kFlush / 16, stream));
+        SSPMV_TRY(dalloc(&fw, kFlush, stream));
+        SSPMV_TRY(dalloc(&sink, 1, stream));
+        SSPMV_CUDA_TRY(cudaMemsetAsync(src, 0, (size_t)std::max<int64_t>(nr, 1) * 16, cu(stream)));
+        SSPMV_CUDA_TRY(cudaMemsetAsync(fr, 0, kFlush, cu(stream)));
+        SSPMV_CUDA_TRY(cudaEventCreate(&e0));
+        SSPMV_CUDA_TRY(cudaEventCreate(&e1));
+        const unsigned grid = (unsigned)(num_sms() * 16);
+        for (int rep = 0; rep < 10; rep++) {  // 3 warm-up runs, median of 7 timed
+            SSPMV_CUDA_TRY(cudaMemsetAsync(fw, rep & 0xff, kFlush, cu(stream)));
+            flush_read<<<(unsigned)(num_sms() * 8), kBlockG, 0, cu(stream)>>>(fr, (int64_t)(kFlush / 16), sink);
+            SSPMV_LAUNCH_CHECK();
+            SSPMV_CUDA_TRY(cudaEventRecord(e0, cu(stream)));
+            stream_kernel<<<grid, kBlockG, 0, cu(stream)>>>(src, nr, dst, nw, sink);
+            SSPMV_LAUNCH_CHECK();
+            SSPMV_CUDA_TRY(cudaEventRecord(e1, cu(stream)));
+            SSPMV_CUDA_TRY(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            SSPMV_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+            if (rep >= 3) ts.push_back(ms);
+        }
+        return SSPMV_OK;
+    };
+    const sspmv_status st = body();
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    dfree(src, stream);
+    dfree(dst, stream);
+    dfree(fr, stream);
+    dfree(fw, stream);
+    dfree(sink, stream);
+    if (st != SSPMV_OK) return st;
+    cudaStreamSynchronize(cu(stream));
+    std::sort(ts.begin(), ts.end());
+    *ms_out = ts[ts.size() / 2];
+    return SSPMV_OK;
+}
 
 extern "C" sspmv_status sspmv_fp64_ceiling(double *fmas_per_second, sspmv_stream_t stream) {
     if (!fmas_per_second) return fail(SSPMV_INVALID_ARG, "fp64 ceiling: null output");

@@ -264,7 +264,7 @@ __global__ void csr_merge_fixup(int64_t num_tiles, int m, const int32_t *__restr
 constexpr int kVecHoist = 6;
 
 template <typename V, int K, int VS, bool PLAIN = false>
-__global__ void __launch_bounds__(kBlock) csr_vector_kernel(
+__global__ void __launch_bounds__(kBlock, (VS == 1 && K == 1) ? (sizeof(V) == 4 ? 6 : 5) : 1) csr_vector_kernel(
     int m, const int32_t *__restrict__ row_offset, const int32_t *__restrict__ col_index,
     const V *__restrict__ values, const V *__restrict__ x, int64_t ldx, int xvec, V alpha, V beta,
     V *__restrict__ y, int64_t ldy) {

@@ -32,3 +32,16 @@ def test_gather_ceiling_checksum(dt):
 
 def test_fp64_ceiling_positive():
     assert bench.Probes().fp64_ceiling() > 1e9
+
+
+def test_stream_ceiling_scales_with_bytes():
+    """A plain stream of 4x the bytes takes longer, and no stream beats the
+    measured HBM peak by more than the burst margin."""
+    import json
+    p = bench.Probes()
+    small = p.stream_ceiling_ms(64 << 20, 8 << 20)
+    large = p.stream_ceiling_ms(256 << 20, 32 << 20)
+    assert 0 < small < large
+    peak = json.loads((bench.ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"] \
+        if (bench.ROOT / "MEASURED_PEAKS.json").exists() else 6800.0
+    assert (288 << 20) / (large * 1e-3) / 1e9 < 1.3 * peak
