@@ -430,6 +430,17 @@ def run_suite(args, dev, rank, world):
             if key not in ceiling:
                 ceiling[key] = probes.gather_ceiling(np_dtype(c["dt"]), c["cols"], min(c["nnz"], 1 << 28))[0]
             pc["gather_frac"] = round(c["nnz"] / (pc["ms"] * 1e-3) / ceiling[key], 4)
+        # the same bytes as a plain stream, cold: what a kernel of each case's
+        # size reaches when it only moves data (short kernels do not reach
+        # the multi-gigabyte copy's bandwidth)
+        streams = {}
+        for c, pc in zip(cases, per_case):
+            yb = c["rows"] * (8 if c["dt"] == "f64" else 4)
+            key = (int(c["bytes"]) - yb, yb)
+            if key not in streams:
+                streams[key] = probes.stream_ceiling_ms(*key)
+            pc["stream_same_bytes_ms"] = round(streams[key], 5)
+            pc["stream_frac"] = round(streams[key] / pc["ms"], 4)
         # FP64: one FMA per nonzero against the device's measured FP64 FMA rate
         fma_rate = probes.fp64_ceiling()
         for c, pc in zip(cases, per_case):
@@ -443,6 +454,7 @@ def run_suite(args, dev, rank, world):
             "frac": round(kernel_rate / rate, 4),
             "what": "one x gather per nonzero; ceiling = random gathers from a vector of the same size, "
                     "indices streamed (benchmark probe sspmv_gather_ceiling)"}
+        roofline["stream_same_bytes_frac"] = per_case[dom]["stream_frac"]
         if dc["dt"] == "f64":
             roofline["fp64_ceiling"] = {
                 "ceiling_fmas_per_s": round(fma_rate, 1), "achieved_fmas_per_s": round(kernel_rate, 1),
@@ -946,6 +958,8 @@ def headline(out: dict) -> dict:
         for extra in ("gather_ceiling", "fp64_ceiling"):
             if rf.get(extra):
                 h["roofline"][extra + "_frac"] = rf[extra]["frac"]
+        if rf.get("stream_same_bytes_frac") is not None:
+            h["roofline"]["stream_same_bytes_frac"] = rf["stream_same_bytes_frac"]
     h["cpu_baseline"] = out.get("cpu_baseline")
     h["clocks"] = out.get("clocks")
     h["gpu_launches"] = out.get("gpu_launches")
