@@ -363,7 +363,10 @@ sspmv_status sspmv_delete_coo(sspmv_coo *A);
  * = defaults (10240, 64/sizeof(value)); more diagonals -> SSPMV_INFEASIBLE. */
 sspmv_status sspmv_csr_to_dia(const sspmv_csr *csr, int32_t max_diags, int32_t alignment, sspmv_dia *out,
                               sspmv_stream_t stream);
-/* LeSpMV_dia (src/spmv_dia.cpp:177-197) */
+/* LeSpMV_dia (src/spmv_dia.cpp:177-197).  kernel_flag 0 (default): a thread
+ * per row over the diagonals; 1 (one right-hand side, at most 16 diagonals):
+ * the rows' values and each diagonal's x window staged in shared memory by
+ * bulk copies, a tile ahead of the threads. */
 sspmv_status sspmv_LeSpMV_dia(double alpha, const sspmv_dia *A, const void *x, double beta, void *y,
                               sspmv_stream_t stream);
 sspmv_status sspmv_spmm_dia(double alpha, const sspmv_dia *A, int32_t k, const void *X, int64_t ldx,

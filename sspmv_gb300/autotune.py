@@ -95,7 +95,8 @@ SLICED_CAPS = [(0, 0), (0, 16), (0, 32), (0, 64), (0, 128)]
 # Kernel candidates per format (formats with one kernel are not listed).
 KERNEL_CANDIDATES = {"csr": CSR_CANDIDATES, "coo": [(0, 0), (1, 0)], "sell": SLICED_CAPS,
                      "sell_c_sigma": SLICED_CAPS, "sell_c_R": SLICED_CAPS,
-                     "bsr": [(0, 0), (1, 0), (2, 0)]}  # BSR: default choice, thread-per-row, block-stream
+                     "bsr": [(0, 0), (1, 0), (2, 0)],  # BSR: default choice, thread-per-row, block-stream
+                     "dia": [(0, 0), (1, 0)]}  # DIA: thread per row, x windows staged by bulk copies
 
 
 def conversion_candidates(fmt: str, num_rows: int) -> list[dict]:

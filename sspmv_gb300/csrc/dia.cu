@@ -15,8 +15,10 @@
 // (the reference scatters into y with atomics, one OpenMP task per diagonal).
 // Column bound is num_cols (the reference uses num_rows, wrong when not square).
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
+#include "bulk.cuh"
 #include "common.cuh"
 #include "plan.cuh"
 #include "primitives.cuh"
@@ -160,9 +162,190 @@ __global__ void __launch_bounds__(kBlock) dia_spmv_kernel(int m, int n, int nd, 
     }
 }
 
+// ------------------------------------------------------------ x staging --
+// kernel_flag 1 (k = 1, at most kDiaStageMax diagonals): rows in tiles of
+// kBlock, CTA g taking tiles g, g + G, ... of a persistent grid.  For a tile,
+// thread 0 streams into one of two shared-memory stages, with bulk copies
+// (cp.async.bulk) completed on the stage's mbarrier: each diagonal's values of
+// the tile's rows, and each diagonal's x window x[r0 + offset_d, ... + tile)
+// (rounded out to 16 bytes, cut at the ends of x).  A tile ahead of the
+// threads; the threads then read values and x from shared memory only (an
+// element outside the staged ranges -- the array's ragged end -- comes from
+// global memory), one FMA per stored element in diagonal order, as the
+// thread-per-row kernel.  Waits are bounded (kMaxPolls); a wait that gives up
+// is counted (sspmv_wait_timeouts) and the CTA leaves after its other copies.
+constexpr int kDiaStageMax = 16;
+constexpr int kDiaStages = 2;
+
+__device__ unsigned long long g_dia_wait_timeouts = 0;
+
+template <typename V>
+struct DiaStage {
+    static constexpr int kPerV = 16 / (int)sizeof(V);
+    static constexpr int kWin = kBlock + 2 * kPerV;          // x window capacity (elements)
+    static constexpr size_t kDataBytes = (size_t)kBlock * sizeof(V);
+    static constexpr size_t kWinBytes = (size_t)kWin * sizeof(V);
+    static size_t bytes(int nd) { return (size_t)nd * (kDataBytes + kWinBytes) + 16 + 2 * kDiaStageMax * 4 + 16; }
+};
+
+template <typename V, bool PLAIN>
+__global__ void __launch_bounds__(kBlock) dia_staged_kernel(int m, int n, int nd, int64_t stride,
+                                                          const int64_t *__restrict__ offsets,
+                                                          const V *__restrict__ data, const V *__restrict__ x,
+                                                          V alpha, V beta, V *__restrict__ y, size_t stage_bytes) {
+    using St = DiaStage<V>;
+    constexpr int kPerV = St::kPerV;
+    extern __shared__ __align__(16) unsigned char dia_smem[];
+    __shared__ int64_t soff[kDiaStageMax];
+    uint64_t *bars = reinterpret_cast<uint64_t *>(dia_smem + kDiaStages * stage_bytes);
+    auto sdata = [&](int st, int d) {
+        return reinterpret_cast<V *>(dia_smem + st * stage_bytes + (size_t)d * St::kDataBytes);
+    };
+    auto swin = [&](int st, int d) {
+        return reinterpret_cast<V *>(dia_smem + st * stage_bytes + (size_t)nd * St::kDataBytes +
+                                     (size_t)d * St::kWinBytes);
+    };
+    // header: [0] r0, [1] rows, [2] rows staged; then a[nd], b[nd] window bounds
+    auto shdr = [&](int st) {
+        return reinterpret_cast<int32_t *>(dia_smem + st * stage_bytes + (size_t)nd * (St::kDataBytes + St::kWinBytes));
+    };
+    const int t = threadIdx.x;
+    const int64_t G = gridDim.x, g = blockIdx.x;
+    const int64_t tiles = ((int64_t)m + kBlock - 1) / kBlock;
+    if (t < nd) soff[t] = offsets[t];
+    if (t == 0) {
+        for (int st = 0; st < kDiaStages; st++) mbar_init(&bars[st], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    auto issue = [&](int64_t k) {  // thread 0: tile g + k G into stage k % kDiaStages
+        const int64_t tile = g + k * G;
+        if (tile >= tiles) return;
+        const int st = (int)(k % kDiaStages);
+        const int64_t r0 = tile * kBlock;
+        const int rows = (int)min((int64_t)kBlock, (int64_t)m - r0);
+        const int staged = rows / kPerV * kPerV;  // values copied: whole 16-byte words of the tile
+        int32_t *h = shdr(st);
+        h[0] = (int)r0;
+        h[1] = rows;
+        h[2] = staged;
+        uint32_t tx = (uint32_t)((size_t)nd * staged * sizeof(V));
+        const int64_t nfloor = (int64_t)n / kPerV * kPerV;
+        for (int d = 0; d < nd; d++) {
+            const int64_t lo = max(r0 + soff[d], (int64_t)0), hi = min(r0 + soff[d] + rows, (int64_t)n);
+            int64_t a = 0, b = 0;
+            if (hi > lo) {
+                a = lo / kPerV * kPerV;
+                b = min((hi + kPerV - 1) / kPerV * kPerV, nfloor);
+                if (b < a) b = a;
+            }
+            h[3 + d] = (int)a;
+            h[3 + kDiaStageMax + d] = (int)b;
+            tx += (uint32_t)((b - a) * (int64_t)sizeof(V));
+        }
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&bars[st], tx);
+        for (int d = 0; d < nd; d++) {
+            if (staged > 0)
+                bulk_g2s(sdata(st, d), data + (int64_t)d * stride + r0, (uint32_t)(staged * sizeof(V)), &bars[st]);
+            const int a = h[3 + d], b = h[3 + kDiaStageMax + d];
+            if (b > a) bulk_g2s(swin(st, d), x + a, (uint32_t)((int64_t)(b - a) * sizeof(V)), &bars[st]);
+        }
+    };
+
+    if (t == 0)
+        for (int k = 0; k < kDiaStages; k++) issue(k);
+    for (int64_t k = 0;; k++) {
+        const int64_t tile = g + k * G;
+        if (tile >= tiles) break;
+        const int st = (int)(k % kDiaStages);
+        const uint32_t parity = (uint32_t)((k / kDiaStages) & 1);
+        const bool ok = __syncthreads_and(t == 0 ? mbar_wait(&bars[st], parity) : true);
+        if (!ok) {
+            if (t == 0) {
+                atomicAdd(&g_dia_wait_timeouts, 1ull);
+                for (int64_t k2 = k + 1; k2 < k + kDiaStages && g + k2 * G < tiles; k2++)
+                    mbar_wait(&bars[k2 % kDiaStages], (uint32_t)((k2 / kDiaStages) & 1));
+            }
+            return;
+        }
+        if (t != 0) mbar_try_wait(&bars[st], parity);  // acquire the completed phase
+        const int32_t *h = shdr(st);
+        const int r0 = h[0], rows = h[1], staged = h[2];
+        if (t < rows) {
+            const int64_t i = (int64_t)r0 + t;
+            V sum = V(0);
+            for (int d = 0; d < nd; d++) {
+                const int64_t j = i + soff[d];
+                if (j >= 0 && j < n) {
+                    const V av = t < staged ? sdata(st, d)[t] : ld_stream(data + (int64_t)d * stride + i);
+                    const int a = h[3 + d], b = h[3 + kDiaStageMax + d];
+                    const V xv = (j >= a && j < b) ? swin(st, d)[j - a] : ld_x(x + j);
+                    sum += av * xv;
+                }
+            }
+            y[i] = row_out(PLAIN, alpha, sum, beta, y + i);
+        }
+        __syncthreads();  // stage st free
+        if (t == 0) issue(k + kDiaStages);
+    }
+}
+
+// One instantiation per kernel: the shared-memory attribute and the
+// occupancy are the kernel's own.
+template <typename V, bool PLAIN>
+sspmv_status launch_dia_staged(const sspmv_dia *A, V alpha, const V *x, V beta, V *y, size_t stage, size_t smem,
+                               sspmv_stream_t s) {
+    auto kernel = dia_staged_kernel<V, PLAIN>;
+    const int nd = A->complete_ndiags;
+    static std::mutex mu;
+    static size_t allowed = 0;                  // dynamic shared memory the kernel may use so far
+    static int per_sm[kDiaStageMax + 1] = {0};  // resident CTAs per SM, by diagonal count
+    {
+        std::lock_guard<std::mutex> g(mu);
+        if (smem > allowed) {
+            SSPMV_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            allowed = smem;
+        }
+        if (per_sm[nd] == 0) {
+            int c = 0;
+            SSPMV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, kernel, kBlock, smem));
+            per_sm[nd] = c > 0 ? c : 1;
+        }
+    }
+    const int64_t tiles = (A->f.num_rows + kBlock - 1) / kBlock;
+    const int64_t grid = std::min<int64_t>(tiles, (int64_t)num_sms() * per_sm[nd]);
+    kernel<<<(unsigned)grid, kBlock, smem, cu(s)>>>((int)A->f.num_rows, (int)A->f.num_cols, nd, A->stride,
+                                                    A->diag_offsets, (const V *)A->diag_data, x, alpha, beta, y,
+                                                    stage);
+    SSPMV_LAUNCH_CHECK();
+    return SSPMV_OK;
+}
+
+// The staged kernel, or false when it does not apply (k > 1, too many
+// diagonals, arrays not 16-byte aligned, x rows not contiguous).
+template <typename V>
+bool try_dia_staged(const sspmv_dia *A, V alpha, const V *x, int64_t ldx, V beta, V *y, int64_t ldy,
+                    sspmv_stream_t s, sspmv_status *st) {
+    const int nd = A->complete_ndiags;
+    if (A->f.kernel_flag != 1 || nd < 1 || nd > kDiaStageMax || ldx != 1 || ldy != 1) return false;
+    if (((reinterpret_cast<uintptr_t>(A->diag_data) | reinterpret_cast<uintptr_t>(x)) & 15) != 0) return false;
+    if (((int64_t)A->stride * (int64_t)sizeof(V)) % 16 != 0) return false;
+    const size_t stage = DiaStage<V>::bytes(nd);
+    const size_t smem = kDiaStages * stage + kDiaStages * sizeof(uint64_t);
+    if (alpha == V(1) && beta == V(0)) *st = launch_dia_staged<V, true>(A, alpha, x, beta, y, stage, smem, s);
+    else *st = launch_dia_staged<V, false>(A, alpha, x, beta, y, stage, smem, s);
+    return true;
+}
+
 template <typename V, int K>
 sspmv_status launch_dia(const sspmv_dia *A, V alpha, const V *x, int64_t ldx, V beta, V *y, int64_t ldy,
                         sspmv_stream_t s) {
+    if constexpr (K == 1) {
+        sspmv_status st = SSPMV_OK;
+        if (try_dia_staged<V>(A, alpha, x, ldx, beta, y, ldy, s, &st)) return st;
+    }
     const unsigned grid = grid_for(A->f.num_rows, kBlock, (int64_t)num_sms() * 16);
     auto go = [&](auto kernel) {
         kernel<<<grid, kBlock, 0, cu(s)>>>((int)A->f.num_rows, (int)A->f.num_cols, A->complete_ndiags, A->stride,
@@ -283,6 +466,14 @@ extern "C" sspmv_status sspmv_LeSpMV_dia(double alpha, const sspmv_dia *A, const
                                          sspmv_stream_t s) {
     return sspmv_spmm_dia(alpha, A, 1, x, 1, beta, y, 1, s);
 }
+
+namespace sspmv {
+// Bounded waits of the staged DIA kernel that gave up (sspmv_wait_timeouts).
+sspmv_status dia_wait_timeouts(unsigned long long *out) {
+    SSPMV_CUDA_TRY(cudaMemcpyFromSymbol(out, g_dia_wait_timeouts, sizeof(*out)));
+    return SSPMV_OK;
+}
+}  // namespace sspmv
 
 extern "C" sspmv_status sspmv_dia_export(const sspmv_dia *A, int64_t *diag_offsets, void *diag_data,
                                          sspmv_stream_t s) {

@@ -1796,10 +1796,15 @@ extern "C" sspmv_status sspmv_LeSpMV_csr_noalloc(double alpha, const sspmv_csr *
     });
 }
 
+namespace sspmv {
+sspmv_status dia_wait_timeouts(unsigned long long *out);
+}
+
 extern "C" sspmv_status sspmv_wait_timeouts(int64_t *count) {
     if (!count) return fail(SSPMV_INVALID_ARG, "null output");
-    unsigned long long v = 0;
+    unsigned long long v = 0, w = 0;
     SSPMV_CUDA_TRY(cudaMemcpyFromSymbol(&v, g_csr_wait_timeouts, sizeof(v)));
-    *count = (int64_t)v;
+    SSPMV_TRY(sspmv::dia_wait_timeouts(&w));
+    *count = (int64_t)(v + w);
     return SSPMV_OK;
 }

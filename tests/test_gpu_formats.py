@@ -433,3 +433,44 @@ def test_plain_sum_instantiations(dt, oracle_lib):
         assert np.isfinite(y).all(), name
         ok, mx, _ = tolerance_ok(y.reshape(-1, 1), yr, ab, nr, dt, 1.0, 0.0, None)
         assert ok, f"{name}: max normalised error {mx}"
+
+
+def _banded_rect(dt, m, n, offsets, seed):
+    """Banded rows with the given column offsets, num_cols n (any shape)."""
+    from sspmv_gb300.synth import HostCSR
+    rng = np.random.default_rng(seed)
+    rows, cols = [], []
+    for i in range(m):
+        cs = sorted({i + o for o in offsets if 0 <= i + o < n})
+        rows.append(len(cs))
+        cols.extend(cs)
+    rp = np.concatenate([[0], np.cumsum(rows)]).astype(np.int32)
+    return HostCSR(m, n, rp, np.asarray(cols, np.int32), rng.uniform(-1, 1, int(rp[-1])).astype(dt))
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
+@pytest.mark.parametrize("shape", [(30001, 30001, (0, 1, -1, 2, -2, 1024, -1024, 2048, -2048)),
+                                   (1000, 1537, (0, 3, 700, -5, 1500)),
+                                   (4099, 257, (0, -1, -4000, 7, 200)),
+                                   (255, 255, tuple(range(-8, 8)))],
+                         ids=["banded", "wide", "tall", "sixteen_diags"])
+def test_dia_staged_kernel(shape, dt, oracle_lib):
+    """kernel_flag 1 of DIA (values and x windows staged in shared memory by
+    bulk copies): rows not a multiple of the tile, windows cut at both ends of
+    x, non-square shapes, 16 diagonals; general alpha/beta and y = sum."""
+    from sspmv_gb300 import lespmv as L
+    from sspmv_gb300 import synth
+    m, n, offs = shape
+    A = _banded_rect(dt, m, n, offs, 5)
+    M = L.csr_to_dia(L.csr_from_host(A))
+    M.set_kernel(1, 0)
+    x = synth.vector(n, 0, dt)
+    y0 = synth.vector(m, 4, dt)
+    for alpha, beta, init in ((ALPHA, BETA, y0), (1.0, 0.0, np.full(m, np.nan, dt))):
+        y = to_dev(init)
+        L.LeSpMV(alpha, M, to_dev(x), beta, y)
+        y64, absum = oracle_lib.spmm_ref(A, x, alpha, beta, y0 if beta else None)
+        ok, mx, _ = tolerance_ok(to_host(y), y64, absum, np.diff(A.row_offset), dt, alpha, beta,
+                                 y0 if beta else None)
+        assert ok, f"{shape[:2]} alpha {alpha}: max normalised error {mx}"
+    assert L.wait_timeouts() == 0
