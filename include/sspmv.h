@@ -227,7 +227,8 @@ sspmv_status sspmv_release_plan(sspmv_features *f, sspmv_stream_t stream);
 sspmv_status sspmv_set_kernel(sspmv_features *f, int32_t kernel_flag, int32_t param);
 
 /* Number of bounded device-side waits (a kernel waiting for its own bulk
- * copies into shared memory) that gave up since the library was loaded, on
+ * copies into shared memory: the CSR row-block and the staged DIA kernels)
+ * that gave up since the library was loaded, on
  * the current device.  A wait that gives up leaves its kernel's output
  * incomplete; 0 in every correct run.  No reference counterpart (the
  * reference has no device code).  Synchronizes the device. */
