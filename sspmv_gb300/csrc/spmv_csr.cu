@@ -18,6 +18,7 @@
 //
 // kernel_flag 1: vector-per-row kernel, `lanes` threads per row (2..32,
 // chosen from the mean row length, or set by the autotuner).
+#include <atomic>
 #include <cuda.h>
 #include <mutex>
 #include <type_traits>
@@ -697,16 +698,18 @@ template <typename V, int W, bool PLAIN>
 sspmv_status go_rowblock_k(const sspmv_csr *A, const int2 *blocks, int64_t nb, V alpha, const V *x, int64_t ldx,
                            V beta, V *y, int64_t ldy, sspmv_stream_t s) {
     constexpr size_t smem = rowblock_smem<V, W>();
-    static int per_sm = 0;  // resident CTAs per SM (set once per instantiation)
-    if (per_sm == 0) {
+    // resident CTAs per SM, set once per instantiation after its shared
+    // memory attribute (a thread that reads it non-zero may launch)
+    static std::atomic<int> per_sm{0};
+    if (per_sm.load(std::memory_order_acquire) == 0) {
         SSPMV_CUDA_TRY(cudaFuncSetAttribute(csr_rowblock_kernel<V, W, PLAIN>,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         int n = 0;
         SSPMV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, csr_rowblock_kernel<V, W, PLAIN>, kBlock,
                                                                      smem));
-        per_sm = n > 0 ? n : 1;
+        per_sm.store(n > 0 ? n : 1, std::memory_order_release);
     }
-    const int64_t grid = std::min<int64_t>(nb, (int64_t)num_sms() * per_sm);
+    const int64_t grid = std::min<int64_t>(nb, (int64_t)num_sms() * per_sm.load(std::memory_order_acquire));
     csr_rowblock_kernel<V, W, PLAIN><<<(unsigned)grid, kBlock, smem, cu(s)>>>(
         nb, (int)A->f.num_rows, A->f.num_nnzs, blocks, A->row_offset, A->col_index, (const V *)A->values, x, ldx,
         alpha, beta, y, ldy);
