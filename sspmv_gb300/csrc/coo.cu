@@ -16,6 +16,7 @@
 // (row_sorted == 0) uses a scale pass plus an atomic scatter, like the
 // reference.
 #include <algorithm>
+#include <atomic>
 
 #include "common.cuh"
 #include "plan.cuh"
@@ -575,10 +576,10 @@ sspmv_status coo_pass(const sspmv_coo *A, Plan *p, V alpha, const V *x, int64_t 
         return SSPMV_OK;
     }
     const size_t smem = (size_t)tile * K * sizeof(V) + (size_t)tile * 4;
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<bool> attr{false};  // set after the attribute call returns
+    if (!attr.load(std::memory_order_acquire)) {
         SSPMV_CUDA_TRY(cudaFuncSetAttribute(coo_tile_kernel<V, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr = true;
+        attr.store(true, std::memory_order_release);
     }
     coo_tile_kernel<V, K><<<(unsigned)nt, kBlock, smem, cu(s)>>>(nnz, A->row_index, A->col_index, (const V *)A->values,
                                                                  x, ldx, alpha, beta, y, ldy, ints, ints + nt,

@@ -358,11 +358,11 @@ sspmv_status launch_merge(const sspmv_csr *A, Plan *p, V alpha, const V *x, int6
     SSPMV_TRY(ensure_merge_plan(p, which, A->f.num_rows, A->f.num_nnzs, A->row_offset, A->f.value_type, s));
     MergePlan &mp = p->merge[which];
     const size_t smem = (size_t)MergeShape<K>::tile * K * sizeof(V) + ((size_t)MergeShape<K>::tile + 1) * 4;
-    static bool attr_set = false;
-    if (!attr_set) {
+    static std::atomic<bool> attr_set{false};  // set after the attribute call returns
+    if (!attr_set.load(std::memory_order_acquire)) {
         SSPMV_CUDA_TRY(cudaFuncSetAttribute(csr_merge_kernel<V, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)smem));
-        attr_set = true;
+        attr_set.store(true, std::memory_order_release);
     }
     csr_merge_kernel<V, K><<<(unsigned)mp.num_tiles, kBlock, smem, cu(s)>>>(
         (int)A->f.num_rows, A->row_offset, A->col_index, (const V *)A->values, x, ldx, alpha, beta, y, ldy,
