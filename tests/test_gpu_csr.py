@@ -166,3 +166,40 @@ def test_csr_deterministic():
         LeSpMV_csr(1.0, M, x, 0.0, y)
         outs.append(to_host(y))
     assert all(np.array_equal(outs[0], o) for o in outs[1:])
+
+
+def test_csr_rowblock_window_changes_and_unaligned_arrays(oracle_lib):
+    """The row-block plan is rebuilt when the window changes (back and forth
+    on one matrix), and arrays that are not 16-byte aligned (a CSR wrapped
+    over offset device buffers) run the default kernel instead."""
+    import ctypes as C
+    import torch
+    from sspmv_gb300 import _lib, synth
+    from sspmv_gb300.lespmv import CSR_Matrix, LeSpMV_csr
+    A = synth.generate(synth.banded(40000), 3, np.float64)
+    x = synth.vector(A.num_cols, 0)
+    y64, absum = oracle_lib.spmm_ref(A, x, 1.0, 0.0)
+    M = _csr(A)
+    for w in (512, 4096, 1024, 512, 2048):
+        M.set_kernel(3, w)
+        y = to_dev(np.full(A.num_rows, np.nan))
+        LeSpMV_csr(1.0, M, to_dev(x), 0.0, y)
+        ok, mx, _ = tolerance_ok(to_host(y), y64, absum, np.diff(A.row_offset), np.float64)
+        assert ok, f"window {w}: {mx}"
+    # the same arrays one element into larger buffers: 4-byte and 8-byte aligned only
+    rp = torch.zeros(A.num_rows + 2, dtype=torch.int32, device="cuda")
+    ci = torch.zeros(A.nnz + 1, dtype=torch.int32, device="cuda")
+    cv = torch.zeros(A.nnz + 1, dtype=torch.float64, device="cuda")
+    rp[1:].copy_(torch.from_numpy(A.row_offset))
+    ci[1:].copy_(torch.from_numpy(A.col_index))
+    cv[1:].copy_(torch.from_numpy(A.values))
+    s = _lib.Csr()
+    _lib.call("sspmv_csr_wrap", C.byref(s), _lib.F64, A.num_rows, A.num_cols, A.nnz, C.c_void_p(rp[1:].data_ptr()),
+              C.c_void_p(ci[1:].data_ptr()), C.c_void_p(cv[1:].data_ptr()))
+    W = CSR_Matrix(s)
+    W.set_kernel(3, 0)
+    y = to_dev(np.full(A.num_rows, np.nan))
+    LeSpMV_csr(1.0, W, to_dev(x), 0.0, y)
+    ok, mx, _ = tolerance_ok(to_host(y), y64, absum, np.diff(A.row_offset), np.float64)
+    assert ok, mx
+    _lib.call("sspmv_release_plan", C.byref(W.s.f), None)

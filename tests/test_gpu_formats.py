@@ -474,3 +474,19 @@ def test_dia_staged_kernel(shape, dt, oracle_lib):
                                  y0 if beta else None)
         assert ok, f"{shape[:2]} alpha {alpha}: max normalised error {mx}"
     assert L.wait_timeouts() == 0
+
+
+def test_dia_staged_falls_back_past_sixteen_diagonals(oracle_lib):
+    """kernel_flag 1 with 17 diagonals runs the thread-per-row kernel."""
+    from sspmv_gb300 import lespmv as L
+    from sspmv_gb300 import synth
+    A = _banded_rect(np.float64, 5000, 5000, tuple(range(-8, 9)), 6)
+    M = L.csr_to_dia(L.csr_from_host(A))
+    assert M.s.complete_ndiags == 17
+    M.set_kernel(1, 0)
+    x = synth.vector(5000, 0)
+    y = to_dev(np.zeros(5000))
+    L.LeSpMV(1.0, M, to_dev(x), 0.0, y)
+    y64, absum = oracle_lib.spmm_ref(A, x, 1.0, 0.0)
+    ok, mx, _ = tolerance_ok(to_host(y), y64, absum, np.diff(A.row_offset), np.float64)
+    assert ok, mx
