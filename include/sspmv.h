@@ -256,6 +256,10 @@ sspmv_status sspmv_delete_csr(sspmv_csr *A);
  * kernel; 1: vector-per-row kernel (param: lanes per row, 1..32); 3: row-block
  * kernel for matrices whose rows all have at most 64 nonzeros (one CTA per
  * block of whole rows, param: nonzeros per block window, 512..4096; one
+ * right-hand side; other matrices and k > 1 run the default kernel); 4:
+ * software-pipelined thread-per-row kernel for matrices whose rows all have
+ * at most 12 nonzeros (each thread keeps three rows' loads in flight; param
+ * 0: values loaded with the x gathers, 1: values loaded one row ahead; one
  * right-hand side; other matrices and k > 1 run the default kernel). */
 sspmv_status sspmv_LeSpMV_csr(double alpha, const sspmv_csr *A, const void *x, double beta, void *y,
                               sspmv_stream_t stream);

@@ -70,7 +70,7 @@ def time_spmv(M, x, y, reps: int = 10, warmup: int = 2, flush=None, stream=None)
 
 
 CSR_CANDIDATES = ([(0, 0), (2, 0)] + [(1, vs) for vs in (1, 2, 4, 8, 16, 32)] +
-                  [(3, w) for w in (512, 1024, 2048, 4096)])
+                  [(3, w) for w in (512, 1024, 2048, 4096)] + [(4, 0), (4, 1)])
 
 
 def tune_kernel(M, x, y, candidates, reps: int = 10) -> dict:

@@ -21,7 +21,7 @@ def _csr(A):
     return csr_from_host(A)
 
 
-@pytest.mark.parametrize("flag", [0, 1, 3])
+@pytest.mark.parametrize("flag", [0, 1, 3, 4])
 @pytest.mark.parametrize("path", CASES, ids=[p.stem for p in CASES])
 def test_csr_golden(path, flag, oracle_lib):
     from sspmv_gb300.lespmv import LeSpMV_csr
@@ -58,7 +58,7 @@ def test_csr_spmm_families(fam, k, dt, oracle_lib):
     X = synth.vector(A.num_cols, 0, dt, k).reshape(A.num_cols, k)
     Y0 = synth.vector(A.num_rows, 7, dt, k).reshape(A.num_rows, k)
     M = _csr(A)
-    for flag in (0, 1, 3):
+    for flag in (0, 1, 3, 4):
         M.kernel_flag = flag
         Y = to_dev(Y0)
         spmm(ALPHA, M, to_dev(X), BETA, Y)
@@ -134,6 +134,77 @@ def test_csr_rowblock_falls_back_on_long_rows(oracle_lib):
     M = _csr(A)
     M.set_kernel(3, 0)
     y = to_dev(np.zeros(A.num_rows))
+    LeSpMV_csr(1.0, M, to_dev(x), 0.0, y)
+    y64, absum = oracle_lib.spmm_ref(A, x, 1.0, 0.0)
+    ok, mx, _ = tolerance_ok(to_host(y), y64, absum, np.diff(A.row_offset), np.float64)
+    assert ok, mx
+
+
+def _rows_up_to(dt, longest, m, seed):
+    """m rows of 0..longest nonzeros (every length present), random columns."""
+    rng = np.random.default_rng(seed)
+    lens = rng.integers(0, longest + 1, m)
+    k = min(m, longest + 1)
+    lens[:k] = np.arange(longest + 1 - k, longest + 1)
+    n = max(m, 64)
+    rp = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    col = np.concatenate([np.sort(rng.choice(n, int(k), replace=False)) for k in lens if k] or
+                         [np.zeros(0, np.int64)]).astype(np.int32)
+    from sspmv_gb300.synth import HostCSR
+    return HostCSR(m, n, rp, col, rng.uniform(-1, 1, int(rp[-1])).astype(dt))
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
+@pytest.mark.parametrize("param", [0, 1])
+@pytest.mark.parametrize("case", ["lap", "banded", "block", "uniform1", "empty_runs_12"] +
+                         [f"rows{h}" for h in (1, 2, 3, 4, 5, 6, 7, 8, 10, 12)] + ["m5", "m40"])
+def test_csr_pipe(case, param, dt, oracle_lib):
+    """kernel_flag 4 (pipelined thread per row) on every template row length
+    (rows of up to 1..12 nonzeros, every length present), the short-row
+    families, runs of empty rows, fewer rows than a warp, with alpha/beta and
+    with alpha = 1, beta = 0 (the y = sum instantiation, y filled with NaN)."""
+    from sspmv_gb300 import synth
+    from sspmv_gb300.lespmv import LeSpMV_csr
+    if case.startswith("rows"):
+        A = _rows_up_to(dt, int(case[4:]), 50000 + 17 * int(case[4:]), int(case[4:]))
+    elif case == "m5":
+        A = _rows_up_to(dt, 7, 5, 1)
+    elif case == "m40":
+        A = _rows_up_to(dt, 12, 40, 2)
+    elif case == "empty_runs_12":
+        A = _empty_runs(dt)
+        lens = np.minimum(np.diff(A.row_offset), 12)
+        keep = np.concatenate([np.arange(A.row_offset[i], A.row_offset[i] + lens[i]) for i in range(A.num_rows)])
+        from sspmv_gb300.synth import HostCSR
+        A = HostCSR(A.num_rows, A.num_cols, np.concatenate([[0], np.cumsum(lens)]).astype(np.int32),
+                    A.col_index[keep], A.values[keep])
+    elif case == "block":
+        A = synth.generate(synth.block(50000, 4, 3000), 3, dt)
+    else:
+        A = synth.generate(_short_rows(synth, case), 3, dt)
+    assert np.diff(A.row_offset).max() <= 12
+    x = synth.vector(A.num_cols, 0, dt)
+    y0 = synth.vector(A.num_rows, 5, dt)
+    M = _csr(A)
+    M.set_kernel(4, param)
+    for alpha, beta, init in ((ALPHA, BETA, y0), (1.0, 0.0, np.full(A.num_rows, np.nan, dt))):
+        y = to_dev(init)
+        LeSpMV_csr(alpha, M, to_dev(x), beta, y)
+        yg = to_host(y)
+        y64, absum = oracle_lib.spmm_ref(A, x, alpha, beta, y0 if beta else None)
+        ok, mx, _ = tolerance_ok(yg, y64, absum, np.diff(A.row_offset), dt, alpha, beta, y0 if beta else None)
+        assert ok, f"{case} param {param} alpha {alpha}: max normalised error {mx}"
+
+
+def test_csr_pipe_falls_back_on_long_rows(oracle_lib):
+    """A row of 13 nonzeros: kernel_flag 4 runs the default kernel."""
+    from sspmv_gb300 import synth
+    from sspmv_gb300.lespmv import LeSpMV_csr
+    A = _rows_up_to(np.float64, 13, 30000, 5)
+    x = synth.vector(A.num_cols, 0)
+    M = _csr(A)
+    M.set_kernel(4, 0)
+    y = to_dev(np.full(A.num_rows, np.nan))
     LeSpMV_csr(1.0, M, to_dev(x), 0.0, y)
     y64, absum = oracle_lib.spmm_ref(A, x, 1.0, 0.0)
     ok, mx, _ = tolerance_ok(to_host(y), y64, absum, np.diff(A.row_offset), np.float64)
