@@ -182,4 +182,22 @@ __device__ __forceinline__ T warp_sum(T v, unsigned width = 32) {
     return v;
 }
 
+// Longest run of consecutive lanes of the warp whose flag is false (all 32
+// lanes call it).  A segmented inclusive scan (Kogge-Stone, a flagged lane
+// starting a segment) needs only the offsets 1, 2, 4, ... up to this run:
+// offsets up to 2^s with 2^(s+1) > run carry a value across run + 1 lanes,
+// the most any lane needs (itself, the unflagged lanes before it and the
+// flagged lane that starts its segment).  Rows that end every few lanes (a
+// few lanes per row) then take two or three scan steps instead of five;
+// in FP64 each step is an add on GB300's narrow FP64 pipe.
+__device__ __forceinline__ int unflagged_run(bool flag) {
+    unsigned z = ~__ballot_sync(0xffffffffu, flag);
+    int run = 0;
+    while (z) {
+        z &= z << 1;
+        run++;
+    }
+    return run;
+}
+
 }  // namespace sspmv

@@ -203,8 +203,11 @@ __global__ void __launch_bounds__(kBlock) coo_tile_kernel(
     int key = b < e ? s_row[e - 1] : -2 - tid;
 
     // block-wide segmented inclusive scan of (key, sum)
+    const int key_up = __shfl_up_sync(0xffffffffu, key, 1);  // every lane shuffles (full mask)
+    const int span = unflagged_run(lane == 0 || key_up != key);
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
+        if (o > span) break;  // warp-uniform
         int k2 = __shfl_up_sync(0xffffffffu, key, o);
         V v2[K];
 #pragma unroll
@@ -403,8 +406,10 @@ __global__ void __launch_bounds__(kBlock, K == 1 ? (sizeof(V) == 4 ? 5 : 4) : 1)
 #pragma unroll
     for (int q = 0; q < K; q++) S[q] = seg[q];
     bool f = any_end;
+    const int span = unflagged_run(f);
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
+        if (o > span) break;  // warp-uniform
         V up[K];
 #pragma unroll
         for (int q = 0; q < K; q++) up[q] = __shfl_up_sync(kFull, S[q], o);

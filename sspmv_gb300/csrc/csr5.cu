@@ -337,8 +337,12 @@ __global__ void __launch_bounds__(kBlock) csr5_tile_kernel(C5View A, const V *__
     }
     // segmented inclusive scan of the lanes' trailing runs, keyed by segment
     int32_t key = rel;
+    // runs of equal keys never cross a tile's lanes (its first lane is flagged)
+    const int32_t key_up = __shfl_up_sync(0xffffffffu, key, 1, OMEGA);  // every lane shuffles (full mask)
+    const int span = unflagged_run(xl == 0 || key_up != key);
 #pragma unroll
     for (int o = 1; o < OMEGA; o <<= 1) {
+        if (o > span) break;  // warp-uniform
         const int32_t k2 = __shfl_up_sync(0xffffffffu, key, o, OMEGA);
         V v2[K];
 #pragma unroll

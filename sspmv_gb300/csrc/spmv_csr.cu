@@ -172,8 +172,11 @@ __device__ __forceinline__ void merge_tile(
 
     // ---- block-wide segmented inclusive scan of carry-outs keyed by row ----
     int key = i0 + ti;
+    const int key_up = __shfl_up_sync(0xffffffffu, key, 1);  // every lane shuffles (full mask)
+    const int span = unflagged_run(lane == 0 || key_up != key);
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
+        if (o > span) break;  // warp-uniform
         int k2 = __shfl_up_sync(0xffffffffu, key, o);
         V v2[K];
 #pragma unroll
@@ -1249,8 +1252,10 @@ __device__ __forceinline__ void stream_chunk_lanes(
 #pragma unroll
     for (int q = 0; q < K; q++) S[q] = seg[q];
     bool f = any_end;
+    const int span = unflagged_run(f);
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
+        if (o > span) break;  // warp-uniform
         V up[K];
 #pragma unroll
         for (int q = 0; q < K; q++) up[q] = __shfl_up_sync(kFull, S[q], o);
@@ -1402,8 +1407,10 @@ __device__ __forceinline__ void stream_chunk_fast(
 #pragma unroll
     for (int q = 0; q < K; q++) S[q] = seg[q];
     bool f = any_end;
+    const int span = unflagged_run(f);
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
+        if (o > span) break;  // warp-uniform
         V up[K];
 #pragma unroll
         for (int q = 0; q < K; q++) up[q] = __shfl_up_sync(kFull, S[q], o);
