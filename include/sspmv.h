@@ -257,10 +257,12 @@ sspmv_status sspmv_delete_csr(sspmv_csr *A);
  * kernel for matrices whose rows all have at most 64 nonzeros (one CTA per
  * block of whole rows, param: nonzeros per block window, 512..4096; one
  * right-hand side; other matrices and k > 1 run the default kernel); 4:
- * software-pipelined thread-per-row kernel for matrices whose rows all have
- * at most 12 nonzeros (each thread keeps three rows' loads in flight; param
- * 0: values loaded with the x gathers, 1: values loaded one row ahead; one
- * right-hand side; other matrices and k > 1 run the default kernel). */
+ * software-pipelined row kernel (each lane keeps three rows' loads in
+ * flight; param bit 0 set: values loaded one row ahead with the columns,
+ * else with the x gathers; param bits 1-2: log2 of the lanes per row, 1 to
+ * 8; rows of at most 12 nonzeros with one lane per row, 8 per lane with
+ * more; one right-hand side; other matrices and k > 1 run the default
+ * kernel). */
 sspmv_status sspmv_LeSpMV_csr(double alpha, const sspmv_csr *A, const void *x, double beta, void *y,
                               sspmv_stream_t stream);
 sspmv_status sspmv_spmm_csr(double alpha, const sspmv_csr *A, int32_t k, const void *X, int64_t ldx,

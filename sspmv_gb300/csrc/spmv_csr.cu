@@ -31,6 +31,7 @@
 #include "bulk.cuh"
 #include "primitives.cuh"
 #include "spmv_common.cuh"
+#include "csr_pipe.cuh"
 #include "serve.cuh"
 
 namespace sspmv {
@@ -752,181 +753,6 @@ sspmv_status launch_rowblock(const sspmv_csr *A, Plan *p, V alpha, const V *x, i
     case 2048: SSPMV_TRY((go_rowblock<V, 2048>(A, blocks, nb, alpha, x, ldx, beta, y, ldy, s))); break;
     case 4096: SSPMV_TRY((go_rowblock<V, 4096>(A, blocks, nb, alpha, x, ldx, beta, y, ldy, s))); break;
     default: SSPMV_TRY((go_rowblock<V, 1024>(A, blocks, nb, alpha, x, ldx, beta, y, ldy, s))); break;
-    }
-    *launched = true;
-    return SSPMV_OK;
-}
-
-// ------------------------------------------ pipelined thread per row --
-// kernel_flag 4: short rows (none longer than kPipeMaxRow), one thread per
-// row, a persistent grid striding over rows r, r + T, r + 2T, ... (T = the
-// grid's threads).  A short-row SpMV is a chain of three dependent loads per
-// row -- row offsets, then columns, then x -- and with one row per thread
-// the chain's latency, not DRAM bandwidth, sets the time of an 84 MB
-// matrix.  Here each thread keeps three rows in flight: the iteration that
-// finishes row r first issues row r's x gathers (its columns were loaded one
-// iteration earlier), the columns of row r + T (offsets loaded one iteration
-// earlier) and the offsets of row r + 2T, and only then waits for row r's
-// gathers and runs its FMA chain in row order.  Param 0: a row's values are
-// loaded with its gathers, so no value waits in registers across an
-// iteration (more threads per SM); param 1 (EARLY): with its columns, one
-// iteration ahead, off the FMA's critical path (fewer threads per SM).
-// Measured (ncu, L2 flushed): the FP64 1024^2 Laplacian 15.4 us against
-// 19.3 us for the one-lane vector kernel, banded rows of 9 FP64 45 against
-// 57 us; the two param values within a few percent of each other.
-// H (the longest row, rounded up to a template size) sets the hoisted loads
-// per row; lanes past their row's end multiply 0 by 0 (never x: it may hold
-// Inf or NaN), and a warp stops at its longest row.
-constexpr int kPipeMaxRow = 12;
-
-// Resident CTAs per SM the register budget is set for: EARLY keeps a row's
-// values in registers across an iteration (fewer threads, values never on
-// the FMA's critical path); otherwise values come with the gathers.
-template <typename V, int H, bool EARLY>
-constexpr int pipe_min_blocks() {
-    if constexpr (sizeof(V) == 8) return EARLY ? (H > 8 ? 2 : H > 6 ? 3 : 4) : (H > 8 ? 3 : H > 6 ? 4 : H > 5 ? 5 : 6);
-    return EARLY ? (H > 8 ? 4 : 5) : (H > 8 ? 5 : H > 5 ? 6 : 8);
-}
-
-template <typename V, int H, bool EARLY, bool PLAIN>
-__global__ void __launch_bounds__(kBlock, (pipe_min_blocks<V, H, EARLY>())) csr_pipe_kernel(
-    int64_t m, const int32_t *__restrict__ rp, const int32_t *__restrict__ col, const V *__restrict__ val,
-    const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy) {
-    constexpr unsigned kAll = 0xffffffffu;
-    const int64_t T = (int64_t)gridDim.x * blockDim.x;
-    const int lane = threadIdx.x & 31;
-    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    // prologue: row r's offsets (waited for) and columns (values: EARLY),
-    // row r + T's offsets
-    int rs0 = 0, n0 = 0;
-    if (r < m) {
-        rs0 = ld_stream(rp + r);
-        n0 = ld_stream(rp + r + 1) - rs0;
-    }
-    int c0[H];
-    V a0[H];
-#pragma unroll
-    for (int q = 0; q < H; q++) {
-        c0[q] = 0;
-        a0[q] = V(0);
-        if (q < n0) {
-            c0[q] = ld_stream(col + rs0 + q);
-            if constexpr (EARLY) a0[q] = ld_stream(val + rs0 + q);
-        }
-    }
-    int rs1 = 0, re1 = 0;
-    if (r + T < m) {
-        rs1 = ld_stream(rp + r + T);
-        re1 = ld_stream(rp + r + T + 1);
-    }
-#pragma unroll 1
-    for (; r - lane < m; r += T) {
-        V xv[H];
-#pragma unroll
-        for (int q = 0; q < H; q++) {
-            xv[q] = V(0);
-            if (q < n0) {
-                xv[q] = ld_x(x + (int64_t)c0[q] * ldx);
-                if constexpr (!EARLY) a0[q] = ld_stream(val + rs0 + q);
-            }
-        }
-        const int n1 = re1 - rs1;
-        int c1[H];
-        V a1[H];
-#pragma unroll
-        for (int q = 0; q < H; q++) {
-            c1[q] = 0;
-            a1[q] = V(0);
-            if (q < n1) {
-                c1[q] = ld_stream(col + rs1 + q);
-                if constexpr (EARLY) a1[q] = ld_stream(val + rs1 + q);
-            }
-        }
-        int rs2 = 0, re2 = 0;
-        if (r + 2 * T < m) {
-            rs2 = ld_stream(rp + r + 2 * T);
-            re2 = ld_stream(rp + r + 2 * T + 1);
-        }
-        const int wmax = __reduce_max_sync(kAll, n0);
-        V sum = V(0);
-#pragma unroll
-        for (int q = 0; q < H; q++)
-            if (q < wmax) sum = fma(a0[q], xv[q], sum);
-        if (r < m) {
-            V *yp = y + r * ldy;
-            *yp = row_out(PLAIN, alpha, sum, beta, yp);
-        }
-#pragma unroll
-        for (int q = 0; q < H; q++) {
-            c0[q] = c1[q];
-            a0[q] = EARLY ? a1[q] : V(0);
-        }
-        rs0 = rs1;
-        n0 = n1;
-        rs1 = rs2;
-        re1 = re2;
-    }
-}
-
-template <typename V, int H, bool EARLY, bool PLAIN>
-sspmv_status go_pipe_k(const sspmv_csr *A, V alpha, const V *x, int64_t ldx, V beta, V *y, int64_t ldy,
-                       sspmv_stream_t s) {
-    // resident CTAs per SM, found once per instantiation
-    static std::atomic<int> per_sm{0};
-    if (per_sm.load(std::memory_order_acquire) == 0) {
-        int n = 0;
-        SSPMV_CUDA_TRY(
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, csr_pipe_kernel<V, H, EARLY, PLAIN>, kBlock, 0));
-        per_sm.store(n > 0 ? n : 1, std::memory_order_release);
-    }
-    const int64_t m = A->f.num_rows;
-    const unsigned grid = grid_for(m, kBlock, (int64_t)num_sms() * per_sm.load(std::memory_order_acquire));
-    csr_pipe_kernel<V, H, EARLY, PLAIN><<<grid, kBlock, 0, cu(s)>>>(m, A->row_offset, A->col_index,
-                                                                    (const V *)A->values, x, ldx, alpha, beta, y, ldy);
-    SSPMV_LAUNCH_CHECK();
-    return SSPMV_OK;
-}
-
-template <typename V, int H>
-sspmv_status go_pipe(const sspmv_csr *A, bool early, V alpha, const V *x, int64_t ldx, V beta, V *y, int64_t ldy,
-                     sspmv_stream_t s) {
-    const bool plain = alpha == V(1) && beta == V(0);
-    if (early)
-        return plain ? go_pipe_k<V, H, true, true>(A, alpha, x, ldx, beta, y, ldy, s)
-                     : go_pipe_k<V, H, true, false>(A, alpha, x, ldx, beta, y, ldy, s);
-    return plain ? go_pipe_k<V, H, false, true>(A, alpha, x, ldx, beta, y, ldy, s)
-                 : go_pipe_k<V, H, false, false>(A, alpha, x, ldx, beta, y, ldy, s);
-}
-
-// Plan slot extra_i[7] = longest row + 1 (0: not yet measured).  Sets
-// *launched = false when a row is longer than kPipeMaxRow.
-template <typename V>
-sspmv_status launch_pipe(const sspmv_csr *A, Plan *p, bool early, V alpha, const V *x, int64_t ldx, V beta, V *y,
-                         int64_t ldy, sspmv_stream_t s, bool *launched) {
-    *launched = false;
-    if (p->extra_i[7] == 0) {
-        std::lock_guard<PlanMutex> g(plan_mutex());
-        if (p->extra_i[7] == 0) {
-            int32_t longest = 0;
-            SSPMV_TRY(max_row_length(A->row_offset, A->f.num_rows, &longest, s));
-            p->extra_i[7] = (int64_t)longest + 1;
-        }
-    }
-    const int64_t longest = p->extra_i[7] - 1;
-    if (longest > kPipeMaxRow) return SSPMV_OK;
-    switch (longest) {
-    case 0:
-    case 1:
-    case 2: SSPMV_TRY((go_pipe<V, 2>(A, early, alpha, x, ldx, beta, y, ldy, s))); break;
-    case 3: SSPMV_TRY((go_pipe<V, 3>(A, early, alpha, x, ldx, beta, y, ldy, s))); break;
-    case 4: SSPMV_TRY((go_pipe<V, 4>(A, early, alpha, x, ldx, beta, y, ldy, s))); break;
-    case 5: SSPMV_TRY((go_pipe<V, 5>(A, early, alpha, x, ldx, beta, y, ldy, s))); break;
-    case 6: SSPMV_TRY((go_pipe<V, 6>(A, early, alpha, x, ldx, beta, y, ldy, s))); break;
-    case 7:
-    case 8: SSPMV_TRY((go_pipe<V, 8>(A, early, alpha, x, ldx, beta, y, ldy, s))); break;
-    case 9:
-    case 10: SSPMV_TRY((go_pipe<V, 10>(A, early, alpha, x, ldx, beta, y, ldy, s))); break;
-    default: SSPMV_TRY((go_pipe<V, 12>(A, early, alpha, x, ldx, beta, y, ldy, s))); break;
     }
     *launched = true;
     return SSPMV_OK;
@@ -1722,7 +1548,7 @@ sspmv_status csr_pass(const sspmv_csr *A, Plan *p, V alpha, const V *x, int64_t 
         }
         if (A->f.kernel_flag == 4) {
             bool launched = false;
-            SSPMV_TRY(launch_pipe<V>(A, p, p->param == 1, alpha, x, ldx, beta, y, ldy, s, &launched));
+            SSPMV_TRY(launch_csr_pipe<V>(A, p, alpha, x, ldx, beta, y, ldy, s, &launched));
             if (launched) return SSPMV_OK;
         }
     }
