@@ -212,6 +212,29 @@ def test_csr_pipe(case, param, dt, oracle_lib):
         assert ok, f"{case} param {param} alpha {alpha}: max normalised error {mx}"
 
 
+@pytest.mark.parametrize("flag,param", [(3, 1024), (4, 0), (4, 1), (4, 7)])
+def test_csr_short_row_kernels_strided_single_rhs(flag, param, oracle_lib):
+    """One right-hand side read from and written to every third column of
+    row-major blocks (ldx = ldy = 3): the row-block and pipelined kernels
+    index x and y by their leading dimensions; the other columns stay as
+    they were."""
+    from sspmv_gb300 import synth
+    from sspmv_gb300.lespmv import spmm
+    A = synth.generate(synth.banded(30000), 3, np.float64)
+    X3 = synth.vector(A.num_cols * 3, 0).reshape(A.num_cols, 3)
+    Y3 = synth.vector(A.num_rows * 3, 5).reshape(A.num_rows, 3)
+    M = _csr(A)
+    M.set_kernel(flag, param)
+    Yd = to_dev(Y3)
+    spmm(ALPHA, M, to_dev(X3)[:, 1:2], BETA, Yd[:, 2:3], k=1, ldx=3, ldy=3)
+    Yg = to_host(Yd)
+    y64, absum = oracle_lib.spmm_ref(A, np.ascontiguousarray(X3[:, 1]), ALPHA, BETA, np.ascontiguousarray(Y3[:, 2]))
+    ok, mx, _ = tolerance_ok(Yg[:, 2], y64, absum, np.diff(A.row_offset), np.float64, ALPHA, BETA,
+                             np.ascontiguousarray(Y3[:, 2]))
+    assert ok, mx
+    assert np.array_equal(Yg[:, :2], Y3[:, :2])
+
+
 def test_csr_pipe_falls_back_on_long_rows(oracle_lib):
     """A row of 13 nonzeros: kernel_flag 4 runs the default kernel."""
     from sspmv_gb300 import synth
