@@ -29,6 +29,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import random
 import statistics
 import subprocess
 import sys
@@ -302,7 +303,7 @@ def run_suite(args, dev, rank, world):
                 cases.append({"fam": fam, "fmt": fmt, "dt": dt, "M": M, "x": x, "y": y,
                               "bytes": M.algorithmic_bytes(1, False), "csr": csr, "nnz": A.nnz,
                               "rows": A.num_rows, "cols": A.num_cols})
-    from sspmv_gb300.autotune import L2Flush
+    from sspmv_gb300.autotune import DITHER_CYCLES, L2Flush
     flush = L2Flush(dev)
     stream = torch.cuda.current_stream()
     pinned = {}
@@ -344,9 +345,14 @@ def run_suite(args, dev, rank, world):
         c["csr_bytes"] = c["csr"].algorithmic_bytes(1, False)
     log("tuned")
 
+    sleep = getattr(torch.cuda, "_sleep", None)
+    dither = random.Random(11)
+
     def one_step(record):
         for c in cases:
             flush()
+            if sleep is not None:  # random start phase against the 2.048 us event-timer step (autotune.time_spmv)
+                sleep(dither.randrange(DITHER_CYCLES))
             e0, e1 = record(c)
             e0.record(stream)
             L.LeSpMV(1.0, c["M"], c["x"], 0.0, c["y"], stream)

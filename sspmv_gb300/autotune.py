@@ -44,19 +44,33 @@ class L2Flush:
         torch.sum(self.r, dim=0, out=self.acc)
 
 
+# Longest dithering delay before a timed launch, in GPU clock cycles: a
+# little more than one 2.048 us step of the event timer at 2.07 GHz.
+DITHER_CYCLES = 4608
+
+
 def time_spmv(M, x, y, reps: int = 10, warmup: int = 2, flush=None, stream=None) -> float:
     """Milliseconds of one SpMV (alpha=1, beta=0) with L2 flushed: the mean
     of the middle half of the sorted samples.  CUDA event times come in
-    steps of about 2 us on this GPU; the trimmed mean resolves kernels of
-    tens of microseconds better than the median, which can only take one of
-    those steps."""
+    steps of 2.048 us on this GPU, and a launch that always follows the same
+    flush starts at the same phase of a step, so every sample can land on the
+    same step, up to one step off the true time.  A spin of a random length
+    (0 to one step) between the flush and the start event spreads the phase:
+    the samples then fall on the two steps around the true time in
+    proportion, and their mean converges to it."""
+    import random
     import torch
     stream = stream or torch.cuda.current_stream()
     if flush is None:
         flush = L2Flush(x.device)
+    sleep = getattr(torch.cuda, "_sleep", None)
+    rng = random.Random(7)
     ts = []
     for i in range(warmup + reps):
         flush()
+        if sleep is not None:
+            with torch.cuda.stream(stream):
+                sleep(rng.randrange(DITHER_CYCLES))
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         L.LeSpMV(1.0, M, x, 0.0, y, stream)
