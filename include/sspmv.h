@@ -260,9 +260,10 @@ sspmv_status sspmv_delete_csr(sspmv_csr *A);
  * software-pipelined row kernel (each lane keeps three rows' loads in
  * flight; param bit 0 set: values loaded one row ahead with the columns,
  * else with the x gathers; param bits 1-2: log2 of the lanes per row, 1 to
- * 8; rows of at most 12 nonzeros with one lane per row, 8 per lane with
- * more; one right-hand side; other matrices and k > 1 run the default
- * kernel). */
+ * 8; param bit 3 set: CTAs of 1024 threads instead of 256 where the
+ * register budget allows; rows of at most 12 nonzeros with one lane per row,
+ * 8 per lane with more; one right-hand side; other matrices and k > 1 run
+ * the default kernel). */
 sspmv_status sspmv_LeSpMV_csr(double alpha, const sspmv_csr *A, const void *x, double beta, void *y,
                               sspmv_stream_t stream);
 sspmv_status sspmv_spmm_csr(double alpha, const sspmv_csr *A, int32_t k, const void *X, int64_t ldx,

@@ -8,8 +8,8 @@ append-only JSONL log keyed by matrix and re-apply them without re-measuring.
 
 CSR candidates: stream kernel (default), merge-path kernel, vector kernel with
 1..32 lanes per row, row-block kernel (short rows) with windows of 512..4096
-nonzeros, pipelined row kernel (short rows) with 1..8 lanes per row and either
-value-load point.
+nonzeros, pipelined row kernel (short rows) with 1..8 lanes per row, either
+value-load point and CTAs of 256 or 1024 threads.
 S-ELL / SELL-c-sigma / SELL-c-R: after the layout, the thread-pass cap (the
 cost model's choice against caps of 16..128 slots).
 SELL-c-sigma candidates (re-conversion per point): C in {8,16,32} x sigma in
@@ -85,7 +85,7 @@ def time_spmv(M, x, y, reps: int = 10, warmup: int = 2, flush=None, stream=None)
 
 
 CSR_CANDIDATES = ([(0, 0), (2, 0)] + [(1, vs) for vs in (1, 2, 4, 8, 16, 32)] +
-                  [(3, w) for w in (512, 1024, 2048, 4096)] + [(4, p) for p in range(8)])
+                  [(3, w) for w in (512, 1024, 2048, 4096)] + [(4, p) for p in range(16)])
 
 
 def tune_kernel(M, x, y, candidates, reps: int = 10) -> dict:

@@ -33,25 +33,30 @@
 namespace sspmv {
 namespace {
 
-constexpr int kPipeBlock = 256;
 constexpr int kPipeMaxRow = 12;     // one lane per row
 constexpr int kPipeMaxPerLane = 8;  // more lanes per row
 
-// Resident CTAs per SM the register budget is set for.
+// Resident CTAs of 256 threads per SM the register budget is set for.
 template <typename V, int H, bool EARLY>
 constexpr int pipe_min_blocks() {
     if constexpr (sizeof(V) == 8) return EARLY ? (H > 8 ? 2 : H > 6 ? 3 : 4) : (H > 8 ? 3 : H > 6 ? 4 : H > 5 ? 5 : 6);
     return EARLY ? (H > 8 ? 4 : 5) : (H > 8 ? 5 : H > 5 ? 6 : 8);
 }
 
-template <typename V, int H, int VS, bool EARLY, bool PLAIN>
-__global__ void __launch_bounds__(kPipeBlock, (pipe_min_blocks<V, H, EARLY>())) csr_pipe_kernel(
+// The same budget for CTAs of BLK threads (256 or 1024).
+template <typename V, int H, bool EARLY, int BLK>
+constexpr int pipe_min_ctas() {
+    return pipe_min_blocks<V, H, EARLY>() * 256 / BLK > 0 ? pipe_min_blocks<V, H, EARLY>() * 256 / BLK : 1;
+}
+
+template <typename V, int H, int VS, bool EARLY, bool PLAIN, int BLK>
+__global__ void __launch_bounds__(BLK, (pipe_min_ctas<V, H, EARLY, BLK>())) csr_pipe_kernel(
     int64_t m, const int32_t *__restrict__ rp, const int32_t *__restrict__ col, const V *__restrict__ val,
     const V *__restrict__ x, int64_t ldx, V alpha, V beta, V *__restrict__ y, int64_t ldy) {
     constexpr unsigned kAll = 0xffffffffu;
-    const int64_t T = (int64_t)gridDim.x * (kPipeBlock / VS);
+    const int64_t T = (int64_t)gridDim.x * (BLK / VS);
     const int lane = threadIdx.x & 31, sub = lane % VS, lead = lane / VS;
-    int64_t r = ((int64_t)blockIdx.x * kPipeBlock + threadIdx.x) / VS;
+    int64_t r = ((int64_t)blockIdx.x * BLK + threadIdx.x) / VS;
     // this lane's elements of a row of n nonzeros: sub, sub + VS, ...
     auto share = [&](int n) { return n > sub ? (n - sub + VS - 1) / VS : 0; };
     // prologue: row r's offsets (waited for) and columns (values: EARLY),
@@ -127,43 +132,53 @@ __global__ void __launch_bounds__(kPipeBlock, (pipe_min_blocks<V, H, EARLY>())) 
     }
 }
 
-template <typename V, int H, int VS, bool EARLY, bool PLAIN>
+template <typename V, int H, int VS, bool EARLY, bool PLAIN, int BLK>
 sspmv_status go_pipe_k(const sspmv_csr *A, V alpha, const V *x, int64_t ldx, V beta, V *y, int64_t ldy,
                        sspmv_stream_t s) {
     // resident CTAs per SM, found once per instantiation
     static std::atomic<int> per_sm{0};
     if (per_sm.load(std::memory_order_acquire) == 0) {
         int n = 0;
-        SSPMV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, csr_pipe_kernel<V, H, VS, EARLY, PLAIN>,
-                                                                     kPipeBlock, 0));
+        SSPMV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &n, csr_pipe_kernel<V, H, VS, EARLY, PLAIN, BLK>, BLK, 0));
         per_sm.store(n > 0 ? n : 1, std::memory_order_release);
     }
     const int64_t m = A->f.num_rows;
-    const unsigned grid =
-        grid_for(m * VS, kPipeBlock, (int64_t)num_sms() * per_sm.load(std::memory_order_acquire));
-    csr_pipe_kernel<V, H, VS, EARLY, PLAIN><<<grid, kPipeBlock, 0, cu(s)>>>(
+    const unsigned grid = grid_for(m * VS, BLK, (int64_t)num_sms() * per_sm.load(std::memory_order_acquire));
+    csr_pipe_kernel<V, H, VS, EARLY, PLAIN, BLK><<<grid, BLK, 0, cu(s)>>>(
         m, A->row_offset, A->col_index, (const V *)A->values, x, ldx, alpha, beta, y, ldy);
     SSPMV_LAUNCH_CHECK();
     return SSPMV_OK;
 }
 
+template <typename V, int H, int VS, bool EARLY, int BLK>
+sspmv_status go_pipe_p(const sspmv_csr *A, V alpha, const V *x, int64_t ldx, V beta, V *y, int64_t ldy,
+                       sspmv_stream_t s) {
+    if (alpha == V(1) && beta == V(0)) return go_pipe_k<V, H, VS, EARLY, true, BLK>(A, alpha, x, ldx, beta, y, ldy, s);
+    return go_pipe_k<V, H, VS, EARLY, false, BLK>(A, alpha, x, ldx, beta, y, ldy, s);
+}
+
+// big: CTAs of 1024 threads instead of 256 (a quarter as many CTAs), where
+// the register budget allows four 256-thread CTAs per SM; otherwise 256.
 template <typename V, int H, int VS>
-sspmv_status go_pipe(const sspmv_csr *A, bool early, V alpha, const V *x, int64_t ldx, V beta, V *y, int64_t ldy,
-                     sspmv_stream_t s) {
-    const bool plain = alpha == V(1) && beta == V(0);
-    if (early)
-        return plain ? go_pipe_k<V, H, VS, true, true>(A, alpha, x, ldx, beta, y, ldy, s)
-                     : go_pipe_k<V, H, VS, true, false>(A, alpha, x, ldx, beta, y, ldy, s);
-    return plain ? go_pipe_k<V, H, VS, false, true>(A, alpha, x, ldx, beta, y, ldy, s)
-                 : go_pipe_k<V, H, VS, false, false>(A, alpha, x, ldx, beta, y, ldy, s);
+sspmv_status go_pipe(const sspmv_csr *A, bool early, bool big, V alpha, const V *x, int64_t ldx, V beta, V *y,
+                     int64_t ldy, sspmv_stream_t s) {
+    if (early) {
+        if constexpr (pipe_min_blocks<V, H, true>() >= 4)
+            if (big) return go_pipe_p<V, H, VS, true, 1024>(A, alpha, x, ldx, beta, y, ldy, s);
+        return go_pipe_p<V, H, VS, true, 256>(A, alpha, x, ldx, beta, y, ldy, s);
+    }
+    if constexpr (pipe_min_blocks<V, H, false>() >= 4)
+        if (big) return go_pipe_p<V, H, VS, false, 1024>(A, alpha, x, ldx, beta, y, ldy, s);
+    return go_pipe_p<V, H, VS, false, 256>(A, alpha, x, ldx, beta, y, ldy, s);
 }
 
 // VS > 1: H = the lane's share of the longest row, rounded up to 4 or 8.
 template <typename V, int VS>
-sspmv_status go_pipe_lanes(const sspmv_csr *A, int64_t per_lane, bool early, V alpha, const V *x, int64_t ldx,
-                           V beta, V *y, int64_t ldy, sspmv_stream_t s) {
-    if (per_lane <= 4) return go_pipe<V, 4, VS>(A, early, alpha, x, ldx, beta, y, ldy, s);
-    return go_pipe<V, 8, VS>(A, early, alpha, x, ldx, beta, y, ldy, s);
+sspmv_status go_pipe_lanes(const sspmv_csr *A, int64_t per_lane, bool early, bool big, V alpha, const V *x,
+                           int64_t ldx, V beta, V *y, int64_t ldy, sspmv_stream_t s) {
+    if (per_lane <= 4) return go_pipe<V, 4, VS>(A, early, big, alpha, x, ldx, beta, y, ldy, s);
+    return go_pipe<V, 8, VS>(A, early, big, alpha, x, ldx, beta, y, ldy, s);
 }
 
 }  // namespace
@@ -183,29 +198,30 @@ sspmv_status launch_csr_pipe(const sspmv_csr *A, Plan *p, V alpha, const V *x, i
     const int64_t longest = p->extra_i[7] - 1;
     const bool early = (p->param & 1) != 0;
     const int vs = 1 << ((p->param >> 1) & 3);
+    const bool big = (p->param & 8) != 0;
     if (vs == 1) {
         if (longest > kPipeMaxRow) return SSPMV_OK;
         switch (longest) {
         case 0:
         case 1:
-        case 2: SSPMV_TRY((go_pipe<V, 2, 1>(A, early, alpha, x, ldx, beta, y, ldy, s))); break;
-        case 3: SSPMV_TRY((go_pipe<V, 3, 1>(A, early, alpha, x, ldx, beta, y, ldy, s))); break;
-        case 4: SSPMV_TRY((go_pipe<V, 4, 1>(A, early, alpha, x, ldx, beta, y, ldy, s))); break;
-        case 5: SSPMV_TRY((go_pipe<V, 5, 1>(A, early, alpha, x, ldx, beta, y, ldy, s))); break;
-        case 6: SSPMV_TRY((go_pipe<V, 6, 1>(A, early, alpha, x, ldx, beta, y, ldy, s))); break;
+        case 2: SSPMV_TRY((go_pipe<V, 2, 1>(A, early, big, alpha, x, ldx, beta, y, ldy, s))); break;
+        case 3: SSPMV_TRY((go_pipe<V, 3, 1>(A, early, big, alpha, x, ldx, beta, y, ldy, s))); break;
+        case 4: SSPMV_TRY((go_pipe<V, 4, 1>(A, early, big, alpha, x, ldx, beta, y, ldy, s))); break;
+        case 5: SSPMV_TRY((go_pipe<V, 5, 1>(A, early, big, alpha, x, ldx, beta, y, ldy, s))); break;
+        case 6: SSPMV_TRY((go_pipe<V, 6, 1>(A, early, big, alpha, x, ldx, beta, y, ldy, s))); break;
         case 7:
-        case 8: SSPMV_TRY((go_pipe<V, 8, 1>(A, early, alpha, x, ldx, beta, y, ldy, s))); break;
+        case 8: SSPMV_TRY((go_pipe<V, 8, 1>(A, early, big, alpha, x, ldx, beta, y, ldy, s))); break;
         case 9:
-        case 10: SSPMV_TRY((go_pipe<V, 10, 1>(A, early, alpha, x, ldx, beta, y, ldy, s))); break;
-        default: SSPMV_TRY((go_pipe<V, 12, 1>(A, early, alpha, x, ldx, beta, y, ldy, s))); break;
+        case 10: SSPMV_TRY((go_pipe<V, 10, 1>(A, early, big, alpha, x, ldx, beta, y, ldy, s))); break;
+        default: SSPMV_TRY((go_pipe<V, 12, 1>(A, early, big, alpha, x, ldx, beta, y, ldy, s))); break;
         }
     } else {
         const int64_t per_lane = (longest + vs - 1) / vs;
         if (per_lane > kPipeMaxPerLane) return SSPMV_OK;
         switch (vs) {
-        case 2: SSPMV_TRY((go_pipe_lanes<V, 2>(A, per_lane, early, alpha, x, ldx, beta, y, ldy, s))); break;
-        case 4: SSPMV_TRY((go_pipe_lanes<V, 4>(A, per_lane, early, alpha, x, ldx, beta, y, ldy, s))); break;
-        default: SSPMV_TRY((go_pipe_lanes<V, 8>(A, per_lane, early, alpha, x, ldx, beta, y, ldy, s))); break;
+        case 2: SSPMV_TRY((go_pipe_lanes<V, 2>(A, per_lane, early, big, alpha, x, ldx, beta, y, ldy, s))); break;
+        case 4: SSPMV_TRY((go_pipe_lanes<V, 4>(A, per_lane, early, big, alpha, x, ldx, beta, y, ldy, s))); break;
+        default: SSPMV_TRY((go_pipe_lanes<V, 8>(A, per_lane, early, big, alpha, x, ldx, beta, y, ldy, s))); break;
         }
     }
     *launched = true;

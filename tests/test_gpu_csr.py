@@ -186,12 +186,13 @@ def _pipe_matrix(case, dt):
 
 
 @pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
-@pytest.mark.parametrize("param", list(range(8)))
+@pytest.mark.parametrize("param", list(range(16)))
 @pytest.mark.parametrize("case", ["lap", "banded", "block", "uniform1", "empty_runs_12"] +
                          [f"rows{h}" for h in (1, 2, 3, 4, 5, 6, 7, 8, 10, 12, 16, 32, 64)] + ["m5", "m40"])
 def test_csr_pipe(case, param, dt, oracle_lib):
     """kernel_flag 4 (pipelined row kernel) with each param (bit 0: value-load
-    point; bits 1-2: 1, 2, 4 or 8 lanes per row) on every template row length
+    point; bits 1-2: 1, 2, 4 or 8 lanes per row; bit 3: 1024-thread CTAs) on
+    every template row length
     (rows of up to 1..12, 16, 32, 64 nonzeros, every length present; rows
     longer than a lane count takes run the default kernel), the short-row
     families, runs of empty rows, fewer rows than a warp, with alpha/beta and
