@@ -22,7 +22,10 @@
 // H (the lane's share of the longest row, rounded up to a template size) sets
 // the hoisted loads per row; lanes past their row's end multiply 0 by 0
 // (never x: it may hold Inf or NaN), and a warp's FMA steps stop at its
-// longest share.
+// longest share.  BLK (256 or 1024 threads per CTA) changes only how many
+// CTAs the grid has: with a quarter as many, a launch reaches its first
+// loads sooner (FP64 Laplacian 19.65 against 20.13 us per launch, FP32
+// 14.18 against 15.24 us, dithered CUDA-event times).
 #include <atomic>
 #include <mutex>
 
