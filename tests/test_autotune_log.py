@@ -36,3 +36,18 @@ def test_candidates_cover_the_reference_macros():
     assert any(c["chunkwidth"] == 32 and c["slicewidth"] == 1 << 20 for c in cs)
     assert dict(sigma=0, omega=0) in autotune.conversion_candidates("csr5", 1000)  # CSR5_SIGMA default
     assert (0, 0) in autotune.CSR_CANDIDATES
+
+
+def test_csr_candidates_cover_every_kernel_and_param():
+    """The CSR candidates the tuner times cover every kernel_flag the library
+    has (0 stream, 1 vector, 2 merge-path, 3 row-block, 4 pipelined) and, for
+    the pipelined kernel, every param (bit 0 value-load point, bits 1-2 lanes
+    per row, bit 3 CTA size); each (flag, param) once."""
+    from sspmv_gb300 import autotune
+    cands = autotune.CSR_CANDIDATES
+    assert len(cands) == len(set(cands))
+    assert {f for f, _ in cands} == {0, 1, 2, 3, 4}
+    assert {p for f, p in cands if f == 4} == set(range(16))
+    assert {p for f, p in cands if f == 1} == {1, 2, 4, 8, 16, 32}
+    assert {p for f, p in cands if f == 3} == {512, 1024, 2048, 4096}
+    assert autotune.KERNEL_CANDIDATES["csr"] is cands

@@ -37,8 +37,9 @@ def _fake_out():
                    "max_median_by_format": {f"{m}/{d}": [0.06, 0.001] for m in fmts for d in ("f64", "f32")}},
         "per_format": per,
         "laplacian_1024": {"cold_GBps": 3000.0, "cold_frac_of_measured_peak": 0.45, "cold_ms": 0.027,
+                           "cold_in_stream_ms": 0.0185, "cold_in_stream_frac_of_measured_peak": 0.67,
                            "warm_GBps": 3700.0, "max_norm_err": 0.1, "median_norm_err": 0.01,
-                           "kernel": {"kernel_flag": 1, "param": 2}},
+                           "kernel": {"kernel_flag": 4, "param": 8}},
         "large_powerlaw_16M": {"formats": {f: {f"k{k}": {"GBps": 2000.0, "max_norm_err": 0.05} for k in (1, 8)}
                                            for f in ("csr", "sell_c_sigma")}},
         "serving": {"host": srv, "device": srv},
@@ -58,6 +59,8 @@ def test_headline_is_compact_and_complete():
     assert h["parity"]["max_median_by_format"]["csr/f64"] == [0.06, 0.001]
     assert h["e2e"]["h2d_bytes_per_step"] == 1
     assert h["serving"]["device"]["equal_p99_ratio"]["per_request"] == 0.5
+    lap = h["laplacian_1024"]
+    assert lap["cold_in_stream_frac_of_measured_peak"] == 0.67 and list(lap["kernel"]) == [4, 8]
     assert h["config"]["skipped"] == 14
 
 
